@@ -1,0 +1,351 @@
+"""Benchmark of the GB300 lattice time step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload precision512|default128|plain64]
+
+Metric: cell-updates/s (one cell-update = one full SSP-RK3 step of one
+cell), on the 512^3 precision-study workload by default: periodic 512^3
+lattice, 256 seeded bubbles nucleated at t = 0 (radius 1.15 R_c), eta drawn
+log-uniform in [0.02, 1.0] from the seed, FP32 state with FP64 reductions and
+FP64 con2prim where gamma > 3.  A step is one SSP-RK3 step of the whole
+lattice (three fused stage launches).  The lattice (9.7 GB) is far larger
+than L2, so no flush is needed between steps.
+
+`value` is device-timed with CUDA events on the library's stream, the state
+resident in HBM.  `e2e` is a headless-style solve through the C ABI: the
+initial state is uploaded from pinned host memory, K steps advance with a
+diagnostics readback every 10 steps, and the final state is copied back to
+pinned host memory, all inside the timed region.
+
+`--impl reference` times the CPU restatement of the reference's algorithm
+(the oracle; the reference itself is Rust/WGSL and cannot run here) on all
+host cores, each step one SSP-RK3 step of a 512x512x32 periodic slab.
+
+With --gpus N > 1 (under torchrun) every rank advances its own replica of
+the workload (the lattices are independent; no data-path collective):
+`value` is the sum over ranks, timed by the slowest rank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "bubble-simulation_gb300"))
+
+BYTES_PER_CELL_UPDATE = 192  # compulsory FP32 traffic of the three stages: 48 + 72 + 72
+
+
+def workload(name: str) -> dict:
+    rng = np.random.default_rng(20251203)
+    if name == "precision512":
+        eta = float(math.exp(rng.uniform(math.log(0.02), math.log(1.0))))
+        return dict(name="512^3 periodic, 256 bubbles at t=0 (1.15 R_c), eta log-uniform[0.02,1] "
+                         f"draw {eta:.4f}, FP32 state + FP64 reductions + FP64 con2prim where gamma>3",
+                    grid=(512, 512, 512), bubbles=256, nucleation="simultaneous", duration=1.0,
+                    eta=eta, precision="mixed", seed=1)
+    if name == "default128":
+        return dict(name="128^3 periodic, 12 bubbles, nucleation times uniform over the first 200 steps, "
+                         "eta 0.3, FP32", grid=(128, 128, 128), bubbles=12, nucleation="uniform",
+                    duration=40.0, eta=0.3, precision="single", seed=1)
+    if name == "plain64":
+        return dict(name="64^3 periodic, 1 bubble at the centre (1.15 R_c), eta 0.3, FP32",
+                    grid=(64, 64, 64), bubbles=1, nucleation="centre", duration=1.0, eta=0.3,
+                    precision="single", seed=1)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(wl: str) -> float | None:
+    """DRAM bytes per cell per stage launch from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "stage_fused_traffic.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_cell_update:"):
+            return float(line.split(":")[1])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_spec(bubble, wl: dict):
+    model = bubble.Model(eta=wl["eta"])
+    return bubble.SimulationSpec(model=model, grid=wl["grid"], nucleation=wl["nucleation"],
+                                 bubbles=wl["bubbles"], nucleation_duration=wl["duration"],
+                                 seed=wl["seed"], precision=wl["precision"], math="fast")
+
+
+def cpu_baseline(state, wl: dict, seconds_budget: float = 20.0) -> dict:
+    """Time the FP32 oracle (all host cores) on a 512x512x32 slab of the warmed-up state."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    oracle.build()
+    field, fluid = state
+    nx, ny, nz = wl["grid"]
+    zs = min(32, nz)
+    f = field.reshape(nz, ny, nx, 2)[:zs].reshape(-1, 2)
+    u = fluid.reshape(nz, ny, nx, 4)[:zs].reshape(-1, 4)
+    m = dict(oracle.DEFAULT_MODEL, eta=wl["eta"])
+    sim = oracle.OracleSim((nx, ny, zs), model=m)
+    sim.set_state(f, u)
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        sim.record_step()
+        steps += 1
+        if time.perf_counter() - t0 > seconds_budget * 0.5 or steps >= 8:
+            break
+    dt = time.perf_counter() - t0
+    cells = nx * ny * zs
+    return {"value": cells * steps / dt, "unit": "cell-updates/s", "cores": oracle.lib().oracle_threads(),
+            "kind": "port",
+            "sample": f"{steps} SSP-RK3 step(s) of a {nx}x{ny}x{zs} periodic slab of the warmed-up "
+                      f"{nx}x{ny}x{nz} state, FP32 oracle (reference kernel structure), "
+                      f"{oracle.lib().oracle_threads()} threads"}
+
+
+def run_reference(args, wl: dict, world: int, rank: int) -> int:
+    if rank != 0:
+        return 0
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    oracle.build()
+    nx, ny, _ = wl["grid"]
+    zs = 32
+    m = dict(oracle.DEFAULT_MODEL, eta=wl["eta"])
+    d = oracle.derived(m)
+    sched = oracle.make_schedule(wl["nucleation"], min(wl["bubbles"], 8), d["seed_radius"],
+                                 (nx, ny, zs), wl["duration"], wl["seed"])
+    sim = oracle.OracleSim((nx, ny, zs), model=m, schedule=sched)
+    sim.record_nucleation()
+    for _ in range(args.warmup):
+        sim.record_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sim.record_step()
+    dt = time.perf_counter() - t0
+    cells = nx * ny * zs
+    value = cells * args.steps / dt
+    sample = (f"one SSP-RK3 step of a {nx}x{ny}x{zs} periodic slab per step (FP32 oracle, the "
+              f"reference's kernel structure, {oracle.lib().oracle_threads()} threads)")
+    line = {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": wl["name"], "sample_grid": [nx, ny, zs]},
+            "cpu_baseline": {"value": value, "unit": "cell-updates/s",
+                             "cores": oracle.lib().oracle_threads(), "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="precision512")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    wl = workload(args.workload)
+    world, rank, local = dist_setup()
+
+    if args.impl == "reference":
+        return run_reference(args, wl, world, rank)
+
+    import torch
+
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
+
+    import bubble_gb300 as bubble
+
+    bubble.load()
+    stream = torch.cuda.Stream()
+    sim = bubble.Simulation(make_spec(bubble, wl))
+    sim.set_stream(stream.cuda_stream)
+    cells = sim.cell_count()
+    # warm-up: nucleation at t = 0 plus W steps
+    sim.advance(args.warmup)
+    sim.synchronize()
+    ty, lz = sim.tile()
+
+    def barrier():
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    launches0 = sim.launches()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    with ClockSampler(local) as clocks:
+        with torch.cuda.stream(stream):
+            start.record(stream)
+            sim.advance(args.steps)
+            end.record(stream)
+        end.synchronize()
+    barrier()
+    launches = sim.launches() - launches0
+    ms = start.elapsed_time(end)
+    if pg:
+        t = torch.tensor([ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * cells * args.steps / (ms * 1e-3)
+
+    # e2e through the C ABI: pinned host state in, K steps, report every 10, state out
+    e2e = None
+    if not args.no_e2e:
+        field, fluid = sim.copy_state()
+        pin_f = torch.from_numpy(field).pin_memory()
+        pin_u = torch.from_numpy(fluid).pin_memory()
+        out_f = torch.empty_like(pin_f).pin_memory()
+        out_u = torch.empty_like(pin_u).pin_memory()
+        L = bubble.load()
+        barrier()
+        t0 = time.perf_counter()
+        bubble._lib.check(L.bubble_load_state(sim.handle, pin_f.data_ptr(), pin_u.data_ptr()))
+        done = 0
+        reports = 0
+        while done < args.steps:
+            n = min(10, args.steps - done)
+            sim.advance(n)
+            sim.diagnostics()
+            reports += 1
+            done += n
+        bubble._lib.check(L.bubble_copy_state(sim.handle, out_f.data_ptr(), out_u.data_ptr()))
+        t1 = time.perf_counter()
+        state_bytes = field.nbytes + fluid.nbytes
+        e2e_val = world * cells * args.steps / (t1 - t0)
+        e2e = {"value": e2e_val, "unit": "cell-updates/s",
+               "h2d_bytes_per_step": state_bytes / args.steps,
+               "d2h_bytes_per_step": (state_bytes + reports * 88) / args.steps,
+               "what": "pinned host state -> K steps with diagnostics every 10 -> pinned host state"}
+
+    peak, peak_kind = peaks()
+    achieved = BYTES_PER_CELL_UPDATE * cells / (ms_per_step * 1e-3) / 1e9
+    traffic_per_cell = ncu_traffic(args.workload)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind,
+                "traffic": (traffic_per_cell * cells / 3) if traffic_per_cell else None,
+                "algorithmic_bytes_per_launch": BYTES_PER_CELL_UPDATE * cells / 3,
+                "kernel": "stage_fused_kernel (3 launches per step)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(sim.copy_state(), wl)
+
+    if rank == 0:
+        line = {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic",
+                "config": {"workload": wl["name"], "grid": list(wl["grid"]), "cells": cells,
+                           "tile": [32, ty, lz], "l2": "inputs larger than L2 (no flush)",
+                           "parallelism": f"replicas x{world}" if world > 1 else "single lattice"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": launches, "clocks": clocks.summary()}
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,281 @@
+"""Python face of the GB300 lattice time step (C ABI via ctypes).
+
+Names follow the reference's Rust host: `Model` (src/physics.rs:44-218),
+`make_schedule` (src/physics.rs:248-296), `SimulationSpec`
+(src/gpu/sim.rs:246-255) and `Simulation` (src/gpu/sim.rs:180-1026).  Every
+call goes through lib/libbubble_gb300.so; nothing here computes physics.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+from typing import Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import BubbleError, check, load
+
+__all__ = ["Model", "SimulationSpec", "Simulation", "Diagnostics", "make_schedule", "derived",
+           "validate_model", "stage_slots", "rk3_coefficients", "lattice_bytes", "max_cubic_size",
+           "vram_query", "vram_available", "lattice_budget", "BubbleError", "load"]
+
+
+@dataclass
+class Model:
+    lambda_: float = 0.5
+    eps_ratio: float = 0.3
+    alpha: float = 0.1
+    eta: float = 0.3
+    phi_b: float = 1.0
+    dx: float = 1.0
+    cfl: float = 0.2
+    seed_kind: str = "critical"  # "critical" (factor of R_c) or "cells"
+    seed_value: float = 1.15
+
+    def c(self) -> _lib.Model:
+        return _lib.Model(self.lambda_, self.eps_ratio, self.alpha, self.eta, self.phi_b, self.dx,
+                          self.cfl, _lib.SEED_CRITICAL if self.seed_kind == "critical" else _lib.SEED_CELLS,
+                          self.seed_value)
+
+    @classmethod
+    def from_c(cls, m: _lib.Model) -> "Model":
+        return cls(m.lambda_, m.eps_ratio, m.alpha, m.eta, m.phi_b, m.dx, m.cfl,
+                   "critical" if m.seed_kind == _lib.SEED_CRITICAL else "cells", m.seed_value)
+
+
+def derived(model: Model) -> dict:
+    d = _lib.Derived()
+    check(load().bubble_model_derived(ctypes.byref(model.c()), ctypes.byref(d)))
+    return {n: getattr(d, n) for n, _ in _lib.Derived._fields_}
+
+
+def validate_model(model: Model) -> str | None:
+    rc = load().bubble_model_validate(ctypes.byref(model.c()))
+    return None if rc == _lib.OK else load().bubble_last_error().decode()
+
+
+def make_schedule(mode: str, count: int, radius: float, grid: Sequence[int], duration: float,
+                  seed: int) -> list[tuple]:
+    L = load()
+    g = (ctypes.c_uint32 * 3)(*grid)
+    out = (_lib.Event * max(count, 1))()
+    n = ctypes.c_uint64()
+    check(L.bubble_make_schedule(_lib.NUCLEATION[mode], count, radius, g, duration, seed, out,
+                                 count, ctypes.byref(n)))
+    return [(out[k].time, tuple(out[k].pos), out[k].radius) for k in range(n.value)]
+
+
+def stage_slots(cur: int) -> list[tuple[int, int]]:
+    o = (ctypes.c_uint32 * 6)()
+    check(load().bubble_stage_slots(cur, o))
+    return [(o[0], o[1]), (o[2], o[3]), (o[4], o[5])]
+
+
+def rk3_coefficients() -> list[tuple[float, float]]:
+    o = (ctypes.c_float * 6)()
+    load().bubble_rk3_coefficients(o)
+    return [(o[0], o[1]), (o[2], o[3]), (o[4], o[5])]
+
+
+def lattice_bytes(grid: Sequence[int]) -> int:
+    return load().bubble_lattice_bytes((ctypes.c_uint32 * 3)(*grid))
+
+
+def max_cubic_size(max_buffer_bytes: int, budget_bytes: int | None) -> tuple[int, bool]:
+    side = ctypes.c_uint32()
+    lim = ctypes.c_int32()
+    check(load().bubble_max_cubic_size(max_buffer_bytes, budget_bytes or 0, budget_bytes is not None,
+                                       ctypes.byref(side), ctypes.byref(lim)))
+    return side.value, bool(lim.value)
+
+
+def vram_query() -> _lib.VramInfo:
+    v = _lib.VramInfo()
+    check(load().bubble_vram_query(ctypes.byref(v)))
+    return v
+
+
+def vram_available(capacity: int, budget: int | None = None, used: int | None = None) -> int:
+    v = _lib.VramInfo(capacity, budget or 0, used or 0, int(budget is not None and used is not None))
+    return load().bubble_vram_available(ctypes.byref(v))
+
+
+def lattice_budget(available: int, current_lattice: int) -> int:
+    return load().bubble_lattice_budget(available, current_lattice)
+
+
+@dataclass
+class SimulationSpec:
+    model: Model = field(default_factory=Model)
+    grid: tuple = (192, 192, 192)
+    nucleation: str = "exponential"
+    bubbles: int = 12
+    nucleation_duration: float = 60.0
+    seed: int = 1
+    precision: str = "single"  # single | mixed | double
+    math: str = "fast"  # fast | strict
+
+    def c(self) -> _lib.Spec:
+        return _lib.Spec(self.model.c(), (ctypes.c_uint32 * 3)(*self.grid), _lib.NUCLEATION[self.nucleation],
+                         self.bubbles, self.nucleation_duration, self.seed, _lib.PRECISION[self.precision],
+                         _lib.MATH[self.math])
+
+
+@dataclass
+class Diagnostics:
+    mean_energy: float
+    broken_fraction: float
+    mean_kinetic: float
+    mean_fluid_energy: float
+    max_velocity: float
+    kinetic_fraction: float
+    sum_energy: float
+    sum_broken: float
+    sum_kinetic: float
+    sum_fluid_energy: float
+    mean_energy_f64: float
+    mean_kinetic_f64: float
+    cells: int
+
+
+class Simulation:
+    """The device-resident lattice (src/gpu/sim.rs:180-1026) behind the C ABI."""
+
+    def __init__(self, spec: SimulationSpec):
+        self._L = load()
+        self.spec = spec
+        h = ctypes.c_void_p()
+        check(self._L.bubble_create(ctypes.byref(spec.c()), ctypes.byref(h)))
+        self._h = h
+        self._dtype = np.float64 if spec.precision == "double" else np.float32
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.bubble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    # -- lifecycle ------------------------------------------------------------
+    def reset(self, schedule: list | None = None):
+        if schedule is None:
+            check(self._L.bubble_reset(self._h, None, 0))
+        else:
+            ev = (_lib.Event * max(len(schedule), 1))()
+            for k, (t, pos, r) in enumerate(schedule):
+                ev[k] = _lib.Event(t, (ctypes.c_float * 3)(*pos), r)
+            check(self._L.bubble_reset(self._h, ev, len(schedule)))
+
+    def set_model(self, model: Model):
+        check(self._L.bubble_set_model(self._h, ctypes.byref(model.c())))
+
+    def resize(self, grid: Sequence[int]):
+        check(self._L.bubble_resize(self._h, (ctypes.c_uint32 * 3)(*grid)))
+
+    def set_stream(self, stream_ptr: int | None):
+        check(self._L.bubble_set_stream(self._h, stream_ptr))
+
+    def set_path(self, path: str):
+        check(self._L.bubble_ext_set_path(self._h, _lib.PATH_REFERENCE if path == "reference" else _lib.PATH_FUSED))
+
+    def set_tile(self, ty: int, lz: int):
+        check(self._L.bubble_ext_set_tile(self._h, ty, lz))
+
+    def tile(self) -> tuple[int, int]:
+        ty, lz = ctypes.c_int32(), ctypes.c_int32()
+        check(self._L.bubble_ext_get_tile(self._h, ctypes.byref(ty), ctypes.byref(lz)))
+        return ty.value, lz.value
+
+    # -- stepping -------------------------------------------------------------
+    def record_steps(self, n: int = 1):
+        check(self._L.bubble_record_steps(self._h, n))
+
+    def advance(self, n: int):
+        check(self._L.bubble_advance(self._h, n))
+
+    def synchronize(self):
+        check(self._L.bubble_synchronize(self._h))
+
+    def nucleate_now(self, rng_seed: int):
+        check(self._L.bubble_nucleate_now(self._h, rng_seed))
+
+    def diagnostics(self, allow_nonfinite: bool = False) -> Diagnostics:
+        d = _lib.Diag()
+        rc = self._L.bubble_diagnostics(self._h, ctypes.byref(d))
+        if not (allow_nonfinite and rc == _lib.ERR_NONFINITE):
+            check(rc)
+        return Diagnostics(**{n: getattr(d, n) for n, _ in _lib.Diag._fields_})
+
+    # -- accessors ------------------------------------------------------------
+    @property
+    def time(self) -> float:
+        return self._L.bubble_time(self._h)
+
+    @property
+    def steps(self) -> int:
+        return self._L.bubble_steps(self._h)
+
+    def cell_count(self) -> int:
+        return self._L.bubble_cell_count(self._h)
+
+    def remaining_bubbles(self) -> int:
+        return self._L.bubble_remaining_bubbles(self._h)
+
+    def device_memory_bytes(self) -> int:
+        return self._L.bubble_device_memory_bytes(self._h)
+
+    @property
+    def grid(self) -> tuple:
+        g = (ctypes.c_uint32 * 3)()
+        check(self._L.bubble_get_grid(self._h, g))
+        return tuple(g)
+
+    @property
+    def model(self) -> Model:
+        m = _lib.Model()
+        check(self._L.bubble_get_model(self._h, ctypes.byref(m)))
+        return Model.from_c(m)
+
+    def schedule(self) -> list[tuple]:
+        n = ctypes.c_uint64()
+        check(self._L.bubble_get_schedule(self._h, None, 0, ctypes.byref(n)))
+        ev = (_lib.Event * max(n.value, 1))()
+        check(self._L.bubble_get_schedule(self._h, ev, n.value, ctypes.byref(n)))
+        return [(ev[k].time, tuple(ev[k].pos), ev[k].radius) for k in range(n.value)]
+
+    def launches(self) -> int:
+        return self._L.bubble_ext_launches(self._h)
+
+    def stream_ptr(self) -> int:
+        return self._L.bubble_ext_stream(self._h) or 0
+
+    # -- state ----------------------------------------------------------------
+    def copy_state(self) -> tuple[np.ndarray, np.ndarray]:
+        n = self.cell_count()
+        field = np.empty((n, 2), dtype=self._dtype)
+        fluid = np.empty((n, 4), dtype=self._dtype)
+        fn = self._L.bubble_copy_state_f64 if self._dtype == np.float64 else self._L.bubble_copy_state
+        check(fn(self._h, field.ctypes.data, fluid.ctypes.data))
+        return field, fluid
+
+    def load_state(self, field: np.ndarray, fluid: np.ndarray):
+        n = self.cell_count()
+        field = np.ascontiguousarray(field, dtype=self._dtype).reshape(n, 2)
+        fluid = np.ascontiguousarray(fluid, dtype=self._dtype).reshape(n, 4)
+        fn = self._L.bubble_load_state_f64 if self._dtype == np.float64 else self._L.bubble_load_state
+        check(fn(self._h, field.ctypes.data, fluid.ctypes.data))

@@ -1,0 +1,55 @@
+// FP32 kernels in the strict arithmetic mode.  Built with --fmad=false and
+// IEEE division / square root: every result is bit-identical with a plain
+// IEEE single-precision restatement of the same operations on the CPU.
+// Also holds the kernels whose results must not depend on the mode (init,
+// nucleation, diagnostics).
+#include "launchers.cuh"
+
+namespace bubble {
+namespace launch {
+
+using namespace launch_detail;
+
+cudaError_t init_f32(V2<float> *field, V4<float> *fluid, uint64_t n, float e_ref,
+                     cudaStream_t s) {
+    return init<float>(field, fluid, n, e_ref, s);
+}
+cudaError_t nucleate_f32(V2<float> *field, const V4<float> *bubbles, int count,
+                         const LatticeParams<float> &P, cudaStream_t s) {
+    return nucleate<float>(field, bubbles, count, P, s);
+}
+cudaError_t prim_f32(const V4<float> *fluid, V4<float> *out, uint64_t n,
+                     const LatticeParams<float> &P, cudaStream_t s) {
+    return prim<float>(fluid, out, n, P, s);
+}
+cudaError_t stage_ref_f32(const StageArgs<float> &A, const V4<float> *p,
+                          const LatticeParams<float> &P, cudaStream_t s) {
+    return stage_ref<float>(A, p, P, s);
+}
+cudaError_t stage_fused_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P,
+                                   TileShape shape, bool mixed, cudaStream_t s) {
+    if (shape.tx != 32 || shape.ty != 8) return cudaErrorInvalidValue;
+    if (mixed) return stage_fused<float, false, true, 8>(A, P, shape.lz, s);
+    return stage_fused<float, false, false, 8>(A, P, shape.lz, s);
+}
+cudaError_t diag_f32(const V2<float> *field, const V4<float> *fluid,
+                     const LatticeParams<float> &P, bool mixed, void *partials,
+                     unsigned int *ticket, DiagResult *out, cudaStream_t s) {
+    if (mixed) return diag<float, true>(field, fluid, P, partials, ticket, out, s);
+    return diag<float, false>(field, fluid, P, partials, ticket, out, s);
+}
+
+size_t diag_partials_bytes() { return sizeof(dev::DiagPartial) * dev::kDiagMaxBlocks; }
+int diag_blocks_for(uint64_t cells) { return dev::diag_blocks(cells); }
+
+bool fused_shape_supported(int precision_double, int ty) {
+    return precision_double ? ty == 4 : (ty == 4 || ty == 8);
+}
+size_t fused_smem_bytes(int precision_double, int ty) {
+    if (precision_double) return dev::FusedLayout<double, 32, 4>::bytes;
+    return ty == 4 ? dev::FusedLayout<float, 32, 4>::bytes : dev::FusedLayout<float, 32, 8>::bytes;
+}
+int fused_threads(int ty) { return 32 * (ty + 1); }
+
+}  // namespace launch
+}  // namespace bubble

@@ -1,0 +1,66 @@
+// Host-callable launchers of the kernels in kernels.cuh.
+//
+// Each function is defined in the translation unit whose compiler flags fix
+// its arithmetic (kernels_strict.cu, kernels_fast.cu, kernels_f64.cu); this
+// header is plain C++ so the host driver, compiled by the host compiler,
+// can call them.
+#pragma once
+
+#include <cuda_runtime_api.h>
+
+#include <cstdint>
+
+#include "params.h"
+
+namespace bubble {
+namespace launch {
+
+// Tile shapes compiled for the fused stage kernel (x is always 32 cells).
+// `ty` selects the instantiation; `lz` is a runtime choice.
+bool fused_shape_supported(int precision_double, int ty);
+// Dynamic shared memory of one CTA of the fused kernel.
+size_t fused_smem_bytes(int precision_double, int ty);
+// Threads per CTA of the fused kernel.
+int fused_threads(int ty);
+
+// ---- FP32 (strict translation unit: no FMA contraction) ----------------
+cudaError_t init_f32(V2<float> *field, V4<float> *fluid, uint64_t n, float e_ref,
+                     cudaStream_t s);
+// `bubbles` is a host array of (cx, cy, cz, r0); it is passed by value.
+cudaError_t nucleate_f32(V2<float> *field, const V4<float> *bubbles, int count,
+                         const LatticeParams<float> &P, cudaStream_t s);
+cudaError_t prim_f32(const V4<float> *fluid, V4<float> *prim, uint64_t n,
+                     const LatticeParams<float> &P, cudaStream_t s);
+cudaError_t stage_ref_f32(const StageArgs<float> &A, const V4<float> *prim,
+                          const LatticeParams<float> &P, cudaStream_t s);
+cudaError_t stage_fused_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P,
+                                   TileShape shape, bool mixed, cudaStream_t s);
+cudaError_t diag_f32(const V2<float> *field, const V4<float> *fluid,
+                     const LatticeParams<float> &P, bool mixed, void *partials,
+                     unsigned int *ticket, DiagResult *out, cudaStream_t s);
+
+// ---- FP32 (fast translation unit: FMA, approximate rcp/sqrt) ------------
+cudaError_t stage_fused_f32_fast(const StageArgs<float> &A, const LatticeParams<float> &P,
+                                 TileShape shape, bool mixed, cudaStream_t s);
+
+// ---- FP64 (the FP64 CUDA oracle; no FMA contraction) --------------------
+cudaError_t init_f64(V2<double> *field, V4<double> *fluid, uint64_t n, double e_ref,
+                     cudaStream_t s);
+cudaError_t nucleate_f64(V2<double> *field, const V4<float> *bubbles, int count,
+                         const LatticeParams<double> &P, cudaStream_t s);
+cudaError_t prim_f64(const V4<double> *fluid, V4<double> *prim, uint64_t n,
+                     const LatticeParams<double> &P, cudaStream_t s);
+cudaError_t stage_ref_f64(const StageArgs<double> &A, const V4<double> *prim,
+                          const LatticeParams<double> &P, cudaStream_t s);
+cudaError_t stage_fused_f64(const StageArgs<double> &A, const LatticeParams<double> &P,
+                            TileShape shape, cudaStream_t s);
+cudaError_t diag_f64(const V2<double> *field, const V4<double> *fluid,
+                     const LatticeParams<double> &P, void *partials, unsigned int *ticket,
+                     DiagResult *out, cudaStream_t s);
+
+// Scratch of the diagnostics reduction: partials + ticket.
+size_t diag_partials_bytes();
+int diag_blocks_for(uint64_t cells);
+
+}  // namespace launch
+}  // namespace bubble

@@ -1,0 +1,102 @@
+// Launch helpers shared by the kernel translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+
+#include "kernels.cuh"
+#include "launch.h"
+
+namespace bubble {
+namespace launch_detail {
+
+inline int grid_for(uint64_t n, int threads) {
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    uint64_t blocks = (n + threads - 1) / threads;
+    const uint64_t cap = (uint64_t)sms * 16;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    return (int)blocks;
+}
+
+// cudaFuncSetAttribute once per device and kernel instantiation.
+template <typename Kernel>
+inline cudaError_t ensure_smem(Kernel k, size_t bytes) {
+    static std::atomic<uint64_t> done_mask{0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t bit = 1ull << (dev & 63);
+    if (done_mask.load(std::memory_order_acquire) & bit) return cudaSuccess;
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) done_mask.fetch_or(bit, std::memory_order_acq_rel);
+    return e;
+}
+
+template <typename R>
+cudaError_t init(V2<R> *field, V4<R> *fluid, uint64_t n, R e_ref, cudaStream_t s) {
+    dev::init_kernel<R><<<grid_for(n, 256), 256, 0, s>>>(field, fluid, n, e_ref);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t nucleate(V2<R> *field, const V4<float> *bubbles, int count, const LatticeParams<R> &P,
+                     cudaStream_t s) {
+    const uint64_t n = (uint64_t)P.nx * P.ny * P.nz;
+    for (int first = 0; first < count; first += dev::kNucleateBatch) {
+        dev::BubbleBatch batch;
+        batch.count = count - first < dev::kNucleateBatch ? count - first : dev::kNucleateBatch;
+        batch._pad[0] = batch._pad[1] = batch._pad[2] = 0;
+        for (int k = 0; k < batch.count; ++k) batch.b[k] = bubbles[first + k];
+        dev::nucleate_kernel<R><<<grid_for(n, 256), 256, 0, s>>>(field, batch, P);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+template <typename R>
+cudaError_t prim(const V4<R> *fluid, V4<R> *prim, uint64_t n, const LatticeParams<R> &P,
+                 cudaStream_t s) {
+    dev::prim_kernel<R><<<grid_for(n, 256), 256, 0, s>>>(fluid, prim, n, P);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t stage_ref(const StageArgs<R> &A, const V4<R> *prim, const LatticeParams<R> &P,
+                      cudaStream_t s) {
+    dim3 grid((P.nx + 63) / 64, P.ny, P.nz);
+    dev::stage_ref_kernel<R><<<grid, 64, 0, s>>>(A, prim, P);
+    return cudaGetLastError();
+}
+
+template <typename R, bool FAST, bool MIXED, int TY>
+cudaError_t stage_fused(const StageArgs<R> &A, const LatticeParams<R> &P, int lz, cudaStream_t s) {
+    constexpr int TX = 32;
+    using L = dev::FusedLayout<R, TX, TY>;
+    auto k = dev::stage_fused_kernel<R, FAST, MIXED, TX, TY>;
+    cudaError_t e = ensure_smem(k, L::bytes);
+    if (e != cudaSuccess) return e;
+    if (lz < 1) lz = 1;
+    const int ntx = (P.nx + TX - 1) / TX, nty = (P.ny + TY - 1) / TY;
+    const int nzc = (P.nz + lz - 1) / lz;
+    dim3 grid(ntx * nty, nzc);
+    k<<<grid, L::NT, L::bytes, s>>>(A, P, lz);
+    return cudaGetLastError();
+}
+
+template <typename R, bool MIXED>
+cudaError_t diag(const V2<R> *field, const V4<R> *fluid, const LatticeParams<R> &P,
+                 void *partials, unsigned int *ticket, DiagResult *out, cudaStream_t s) {
+    const uint64_t n = (uint64_t)P.nx * P.ny * P.nz;
+    const int blocks = dev::diag_blocks(n);
+    dev::diag_kernel<R, MIXED><<<blocks, dev::kDiagThreads, 0, s>>>(
+        field, fluid, P, reinterpret_cast<dev::DiagPartial *>(partials), ticket, out);
+    return cudaGetLastError();
+}
+
+}  // namespace launch_detail
+}  // namespace bubble

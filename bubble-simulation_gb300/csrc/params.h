@@ -1,0 +1,65 @@
+// Parameter blocks shared by the host driver and the CUDA kernels.
+//
+// LatticeParams mirrors the `SimParams` uniform (shaders/common.wgsl:25-58,
+// host values src/gpu/sim.rs:613-644) minus the fields no kernel on this path
+// reads (time, vis_gain, padding).  It is templated on the arithmetic type so
+// the FP64 kernels get double constants (each widened exactly from the f32
+// value the host derives, so both precisions solve the same problem).
+#pragma once
+
+#include <cstdint>
+
+#if defined(__CUDACC__)
+#define BUBBLE_HD __host__ __device__ __forceinline__
+#else
+#define BUBBLE_HD inline
+#endif
+
+namespace bubble {
+
+template <typename R>
+struct alignas(4 * sizeof(R)) V4 {
+    R x, y, z, w;
+};
+template <typename R>
+struct alignas(2 * sizeof(R)) V2 {
+    R x, y;
+};
+
+template <typename R>
+struct LatticeParams {
+    int32_t nx, ny, nz, _pad;
+    R dx, inv_dx, eta, lambda;
+    R phi_b, m2, delta, wall_width;
+    R p_floor, e_floor, z_max, e_ref;
+};
+
+// One SSP-RK3 stage: U_out = a0 U^n + a1 (U_in + dt L(U_in))
+// (shaders/common.wgsl:60-68, src/gpu/sim.rs:133-135, 650-656).
+template <typename R>
+struct StageArgs {
+    const V2<R> *field_n;
+    const V4<R> *fluid_n;
+    const V2<R> *field_in;
+    const V4<R> *fluid_in;
+    V2<R> *field_out;
+    V4<R> *fluid_out;
+    R a0, a1, dt;
+    int32_t stage;  // 0, 1, 2; stage 0 has a0 == 0 and never reads U^n
+};
+
+// Result of the diagnostics reduction (shaders/reduce.wgsl:32-38), with FP64
+// sums.
+struct DiagResult {
+    double sums[4];       // e_total, broken, kinetic, E
+    uint32_t max_v_bits;  // bits of max |v| (non-negative f32)
+    uint32_t nonfinite;   // count of blocks that saw a non-finite term
+    uint64_t cells;
+};
+
+// Tile shape of the fused stage kernel.
+struct TileShape {
+    int32_t tx, ty, lz;  // x, y tile (cells) and z chunk (planes)
+};
+
+}  // namespace bubble

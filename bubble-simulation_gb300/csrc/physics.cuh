@@ -1,0 +1,360 @@
+// Device-side physics of one lattice cell and one cell face.
+//
+// Restates, for CUDA, the per-cell arithmetic of the reference shaders:
+//   potential / dpotential         shaders/potential.wgsl:38-47
+//   bag EOS, con2prim, fluxes      shaders/eos.wgsl:94-176
+//   MC limiter                     shaders/common.wgsl:114-136
+//   sanitise, HLL                  shaders/step.wgsl:61-90
+//   nucleation profile             shaders/nucleate.wgsl:51-85
+//
+// Two arithmetic modes share this file:
+//   FAST = false  the WGSL evaluation order with IEEE division and square
+//                 root; the translation units that instantiate it are built
+//                 with --fmad=false, so every result is bit-identical with a
+//                 plain IEEE restatement on the CPU.
+//   FAST = true   the same formulas with shared reciprocals and hardware
+//                 approximate rcp/sqrt/rsqrt (MUFU), built with FMA
+//                 contraction.  Results differ from the strict mode by
+//                 rounding only.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "params.h"
+
+namespace bubble {
+namespace dev {
+
+#define BUBBLE_DEV __device__ __forceinline__
+
+template <typename R>
+BUBBLE_DEV R vmax(R a, R b) {
+    return fmax(a, b);
+}
+template <typename R>
+BUBBLE_DEV R vmin(R a, R b) {
+    return fmin(a, b);
+}
+template <>
+BUBBLE_DEV float vmax<float>(float a, float b) {
+    return fmaxf(a, b);
+}
+template <>
+BUBBLE_DEV float vmin<float>(float a, float b) {
+    return fminf(a, b);
+}
+
+// Hardware approximations used by the FAST mode (float only).
+BUBBLE_DEV float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+BUBBLE_DEV float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+BUBBLE_DEV float rsqrt_approx(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+//  Potential (shaders/potential.wgsl:38-47)
+// ---------------------------------------------------------------------------
+template <typename R>
+BUBBLE_DEV R potential(R phi, const LatticeParams<R> &P) {
+    const R p2 = phi * phi;
+    return R(0.5) * P.m2 * p2 - P.delta * p2 * phi / R(3.0) + R(0.25) * P.lambda * p2 * p2;
+}
+template <typename R>
+BUBBLE_DEV R dpotential(R phi, const LatticeParams<R> &P) {
+    return phi * (P.m2 - P.delta * phi + P.lambda * phi * phi);
+}
+
+// ---------------------------------------------------------------------------
+//  Limiter (shaders/common.wgsl:114-136)
+// ---------------------------------------------------------------------------
+// minmod3(0.5 (dm + dp), 2 dm, 2 dp) with WGSL sign() semantics.  The three
+// signs agree exactly when dm and dp are both non-zero with one sign (the
+// half-sum of two same-signed floats cannot round to zero and doubling keeps
+// the sign), and then sign(a) * min(|a|, |b|, |c|) is that sign applied to
+// the minimum; every other case returns zero.  Same values, fewer
+// instructions.
+template <typename R>
+BUBBLE_DEV R limit_slope(R dm, R dp) {
+    const bool same = (dm > R(0) && dp > R(0)) || (dm < R(0) && dp < R(0));
+    const R a = fabs(R(0.5) * (dm + dp));
+    const R m = vmin(a, vmin(fabs(R(2.0) * dm), fabs(R(2.0) * dp)));
+    return same ? copysign(m, dm) : R(0);
+}
+
+// ---------------------------------------------------------------------------
+//  Bag EOS (shaders/eos.wgsl:94-123): conserved -> primitive
+// ---------------------------------------------------------------------------
+// eos_prim_from_cons(eos_regularise(u)) -> (vx, vy, vz, p).
+template <typename R, bool FAST>
+BUBBLE_DEV V4<R> prim_from_cons(const V4<R> &u, const LatticeParams<R> &P) {
+    const R e_lab = vmax(u.x, P.e_floor);
+    R zx = u.y, zy = u.z, zz = u.w;
+    const R zcap = P.z_max * e_lab;
+    if constexpr (FAST) {
+        const R z2raw = zx * zx + zy * zy + zz * zz;
+        if (z2raw > zcap * zcap) {
+            const R s = zcap * rsqrt_approx(z2raw);
+            zx *= s;
+            zy *= s;
+            zz *= s;
+        }
+        const R z2 = zx * zx + zy * zy + zz * zz;
+        const R disc = vmax(R(4.0) * e_lab * e_lab - R(3.0) * z2, R(0.0));
+        R p = (e_lab * e_lab - z2) * rcp_approx(e_lab + sqrt_approx(disc));
+        p = vmax(p, P.p_floor);
+        const R inv = rcp_approx(vmax(e_lab + p, R(1e-30)));
+        return V4<R>{zx * inv, zy * inv, zz * inv, p};
+    } else {
+        const R zlen = sqrt(zx * zx + zy * zy + zz * zz);
+        if (zlen > zcap) {
+            const R s = zcap / vmax(zlen, R(1e-30));
+            zx = zx * s;
+            zy = zy * s;
+            zz = zz * s;
+        }
+        const R z2 = zx * zx + zy * zy + zz * zz;
+        const R disc = vmax(R(4.0) * e_lab * e_lab - R(3.0) * z2, R(0.0));
+        R p = (e_lab * e_lab - z2) / (e_lab + sqrt(disc));
+        p = vmax(p, P.p_floor);
+        const R s = vmax(e_lab + p, R(1e-30));
+        return V4<R>{zx / s, zy / s, zz / s, p};
+    }
+}
+
+// FP64 recovery of one FP32 cell, used where the Lorentz factor exceeds 3
+// (v^2 > 8/9), the regime where E^2 - Z^2 cancels.
+BUBBLE_DEV V4<float> prim_from_cons_f64(const V4<float> &u, const LatticeParams<float> &P) {
+    const double e_lab = fmax((double)u.x, (double)P.e_floor);
+    double zx = u.y, zy = u.z, zz = u.w;
+    const double zcap = (double)P.z_max * e_lab;
+    const double zlen = sqrt(zx * zx + zy * zy + zz * zz);
+    if (zlen > zcap) {
+        const double s = zcap / fmax(zlen, 1e-30);
+        zx *= s;
+        zy *= s;
+        zz *= s;
+    }
+    const double z2 = zx * zx + zy * zy + zz * zz;
+    const double disc = fmax(4.0 * e_lab * e_lab - 3.0 * z2, 0.0);
+    double p = (e_lab * e_lab - z2) / (e_lab + sqrt(disc));
+    p = fmax(p, (double)P.p_floor);
+    const double s = fmax(e_lab + p, 1e-30);
+    return V4<float>{(float)(zx / s), (float)(zy / s), (float)(zz / s), (float)p};
+}
+
+template <typename R, bool FAST, bool MIXED>
+BUBBLE_DEV V4<R> recover(const V4<R> &u, const LatticeParams<R> &P) {
+    V4<R> q = prim_from_cons<R, FAST>(u, P);
+    if constexpr (MIXED) {
+        const R v2 = q.x * q.x + q.y * q.y + q.z * q.z;
+        if (v2 > R(8.0) / R(9.0)) q = prim_from_cons_f64(u, P);
+    }
+    return q;
+}
+
+// ---------------------------------------------------------------------------
+//  sanitise (shaders/step.wgsl:61-72)
+// ---------------------------------------------------------------------------
+template <typename R>
+BUBBLE_DEV V4<R> sanitise(const V4<R> &q, R p_floor, R vmax2) {
+    const R p = vmax(q.w, p_floor);
+    R vx = q.x, vy = q.y, vz = q.z;
+    const R v2 = vx * vx + vy * vy + vz * vz;
+    if (v2 > vmax2) {
+        const R s = sqrt(vmax2 / vmax(v2, R(1e-30)));
+        vx = vx * s;
+        vy = vy * s;
+        vz = vz * s;
+    }
+    return V4<R>{vx, vy, vz, p};
+}
+
+template <typename R>
+BUBBLE_DEV V4<R> v4_sub(const V4<R> &a, const V4<R> &b) {
+    return V4<R>{a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w};
+}
+
+// limit_slope4 (shaders/common.wgsl:129-136).
+template <typename R>
+BUBBLE_DEV V4<R> limit_slope4(const V4<R> &dm, const V4<R> &dp) {
+    return V4<R>{limit_slope(dm.x, dp.x), limit_slope(dm.y, dp.y), limit_slope(dm.z, dp.z),
+                 limit_slope(dm.w, dp.w)};
+}
+
+// q + 0.5 s and q - 0.5 s (shaders/step.wgsl:135-144).
+template <typename R>
+BUBBLE_DEV V4<R> half_step(const V4<R> &q, const V4<R> &s, R sign) {
+    // sign is +1 or -1; multiplying by it is exact, so this equals q +- 0.5 s.
+    return V4<R>{q.x + sign * (R(0.5) * s.x), q.y + sign * (R(0.5) * s.y),
+                 q.z + sign * (R(0.5) * s.z), q.w + sign * (R(0.5) * s.w)};
+}
+
+// ---------------------------------------------------------------------------
+//  HLL face flux (shaders/step.wgsl:74-90 with eos.wgsl:129-176)
+// ---------------------------------------------------------------------------
+template <int AXIS, typename R>
+BUBBLE_DEV R comp(const V4<R> &q) {
+    if constexpr (AXIS == 0) return q.x;
+    else if constexpr (AXIS == 1) return q.y;
+    else return q.z;
+}
+
+// Per-side quantities of the HLL solver for one sanitised face state.
+template <typename R>
+struct FaceSide {
+    V4<R> u;     // eos_cons_from_prim
+    V4<R> f;     // eos_flux along the axis
+    R lm, lp;    // eos_wave_speeds
+};
+
+template <int AXIS, typename R, bool FAST>
+BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2) {
+    FaceSide<R> s;
+    const R vx = q.x, vy = q.y, vz = q.z, p = q.w;
+    const R vd = comp<AXIS>(q);
+    const R v2 = vmin(vx * vx + vy * vy + vz * vz, zmax2);
+    const R cs2 = R(1.0) / R(3.0);  // eos_sound_speed2 (eos.wgsl:50-53)
+    if constexpr (FAST) {
+        const R w = R(4.0) * p * rcp_approx(R(1.0) - v2);
+        s.u = V4<R>{w - p, w * vx, w * vy, w * vz};
+        const R inv_den = rcp_approx(R(1.0) - v2 * cs2);
+        const R vd2 = vd * vd;
+        const R rad = vmax((R(1.0) - v2) * (R(1.0) - vd2 - cs2 * (v2 - vd2)), R(0.0));
+        const R a = vd * (R(1.0) - cs2) * inv_den;
+        const R cs = R(0.57735026918962576451);
+        const R b = cs * sqrt_approx(rad) * inv_den;
+        s.lm = a - b;
+        s.lp = a + b;
+    } else {
+        const R w = R(4.0) * p / (R(1.0) - v2);
+        s.u = V4<R>{w - p, w * vx, w * vy, w * vz};
+        const R cs = sqrt(cs2);
+        const R denom = R(1.0) - v2 * cs2;
+        const R rad = vmax((R(1.0) - v2) * (R(1.0) - vd * vd - cs2 * (v2 - vd * vd)), R(0.0));
+        const R a = vd * (R(1.0) - cs2) / denom;
+        const R b = cs * sqrt(rad) / denom;
+        s.lm = a - b;
+        s.lp = a + b;
+    }
+    s.f = V4<R>{(s.u.x + p) * vd, s.u.y * vd, s.u.z * vd, s.u.w * vd};
+    if constexpr (AXIS == 0) s.f.y = s.f.y + p;
+    if constexpr (AXIS == 1) s.f.z = s.f.z + p;
+    if constexpr (AXIS == 2) s.f.w = s.f.w + p;
+    return s;
+}
+
+// hll_flux(q_l, q_r, axis).  The phi arguments of the reference's hll_flux
+// reach only the bag EOS functions, which ignore them, so they are dropped.
+template <int AXIS, typename R, bool FAST>
+BUBBLE_DEV V4<R> hll_flux(const V4<R> &ql, const V4<R> &qr, R zmax2) {
+    const FaceSide<R> L = face_side<AXIS, R, FAST>(ql, zmax2);
+    const FaceSide<R> Rt = face_side<AXIS, R, FAST>(qr, zmax2);
+    const R s_min = vmin(vmin(L.lm, Rt.lm), R(0.0));
+    const R s_max = vmax(vmax(L.lp, Rt.lp), R(0.0));
+    const R den = vmax(s_max - s_min, R(1e-12));
+    const R smm = s_min * s_max;
+    if constexpr (FAST) {
+        const R inv = rcp_approx(den);
+        return V4<R>{(s_max * L.f.x - s_min * Rt.f.x + smm * (Rt.u.x - L.u.x)) * inv,
+                     (s_max * L.f.y - s_min * Rt.f.y + smm * (Rt.u.y - L.u.y)) * inv,
+                     (s_max * L.f.z - s_min * Rt.f.z + smm * (Rt.u.z - L.u.z)) * inv,
+                     (s_max * L.f.w - s_min * Rt.f.w + smm * (Rt.u.w - L.u.w)) * inv};
+    } else {
+        return V4<R>{(s_max * L.f.x - s_min * Rt.f.x + smm * (Rt.u.x - L.u.x)) / den,
+                     (s_max * L.f.y - s_min * Rt.f.y + smm * (Rt.u.y - L.u.y)) / den,
+                     (s_max * L.f.z - s_min * Rt.f.z + smm * (Rt.u.z - L.u.z)) / den,
+                     (s_max * L.f.w - s_min * Rt.f.w + smm * (Rt.u.w - L.u.w)) / den};
+    }
+}
+
+// ---------------------------------------------------------------------------
+//  Deterministic tanh for the nucleation profile
+// ---------------------------------------------------------------------------
+// tanh(x) = expm1(2|x|) / (expm1(2|x|) + 2) with the sign of x, expm1 from a
+// Taylor series near zero and otherwise from Cody-Waite range reduction by
+// ln 2 (split into the classic high/low parts) and a Taylor polynomial for
+// exp(r), |r| <= ln2/2, scaled by an exact power of two.  Evaluated in FP64
+// with plain IEEE operations only, so a CPU and a GPU build without FMA
+// contraction return identical bits; the FP32 result is the FP64 value
+// rounded once.  Relative error of the FP64 value is below 1e-15.
+BUBBLE_HD double pow2_int(int k) {
+    // k in [0, 1023]
+    const unsigned long long bits = (unsigned long long)(k + 1023) << 52;
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)bits);
+#else
+    double d;
+    __builtin_memcpy(&d, &bits, sizeof(d));
+    return d;
+#endif
+}
+
+BUBBLE_HD double det_expm1_nonneg(double y) {
+    if (y < 0.5) {
+        double r = 1.0;
+        for (int k = 18; k >= 2; --k) r = 1.0 + y * r / (double)k;
+        return y * r;
+    }
+    const double inv_ln2 = 1.44269504088896338700e+00;
+    const double ln2_hi = 6.93147180369123816490e-01;
+    const double ln2_lo = 1.90821492927058770002e-10;
+    const double kf = floor(y * inv_ln2 + 0.5);
+    const double r = (y - kf * ln2_hi) - kf * ln2_lo;
+    double e = 1.0;
+    for (int k = 16; k >= 1; --k) e = 1.0 + r * e / (double)k;
+    return e * pow2_int((int)kf) - 1.0;
+}
+
+BUBBLE_HD double det_tanh(double x) {
+    const double ax = fabs(x);
+    double t;
+    if (ax > 22.0) {
+        t = 1.0;
+    } else {
+        const double em = det_expm1_nonneg(2.0 * ax);
+        t = em / (em + 2.0);
+    }
+    return x < 0.0 ? -t : t;
+}
+
+// Cut-off beyond which the profile is exactly zero: det_tanh rounds to 1.
+template <typename R>
+struct TanhCut;
+template <>
+struct TanhCut<float> {
+    static constexpr float value = 12.0f;
+};
+template <>
+struct TanhCut<double> {
+    static constexpr double value = 22.0;
+};
+
+template <typename R>
+BUBBLE_HD R det_tanh_r(R x) {
+    if (x > TanhCut<R>::value) return R(1);
+    if (x < -TanhCut<R>::value) return R(-1);
+    return (R)det_tanh((double)x);
+}
+
+// min_image (shaders/nucleate.wgsl:51-57).
+template <typename R>
+BUBBLE_DEV R min_image(R d, R n) {
+    R r = d;
+    if (r > R(0.5) * n) r = r - n;
+    if (r < R(-0.5) * n) r = r + n;
+    return r;
+}
+
+}  // namespace dev
+}  // namespace bubble

@@ -1,0 +1,124 @@
+"""Generate the committed golden fixtures from the oracle and the reference's docs.
+
+    python tests/golden/make_golden.py [--reference DIR] [--skip-128]
+
+Writes into tests/golden/:
+  published_numerics.json  the reference's published single-bubble and
+                           quiescent tables, parsed from its docs/NUMERICS.md
+  single_bubble_128.json   the oracle's diagnostics of that published case
+                           (128^3, 1 bubble, simultaneous, seed 1) at step 100,
+                           beside the published row
+  cases.npz                small per-cell cases: initial state, oracle state
+                           after N steps (FP32 and FP64), and the parameters
+
+The reference tree is read only here, at generation time; tests read the
+JSON/NPZ files.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import re
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT / "oracle"))
+import oracle  # noqa: E402
+
+
+def parse_tables(numerics_md: Path) -> dict:
+    text = numerics_md.read_text()
+    out = {"single_bubble": {}, "quiescent": {}}
+    # Single bubble table: step time broken R_eq max|v| K E/E0
+    sb = re.search(r"### Single bubble, default parameters.*?```(.*?)```", text, re.S)
+    for line in sb.group(1).strip().splitlines()[1:]:
+        p = line.split()
+        out["single_bubble"][p[0]] = dict(time=float(p[1]), broken_pct=float(p[2].rstrip("%")),
+                                          r_eq=float(p[3]), max_v=float(p[4]), k=float(p[5]),
+                                          e_ratio=float(p[6]))
+    q = re.search(r"### Quiescent state is exactly preserved.*?```(.*?)```", text, re.S)
+    for line in q.group(1).strip().splitlines()[1:]:
+        p = line.split()
+        out["quiescent"][p[0]] = dict(broken_pct=float(p[1].rstrip("%")), max_v=float(p[2]), k=float(p[3]))
+    return out
+
+
+def perturbed_state(sim: "oracle.OracleSim", seed: int, amp: float) -> None:
+    """Add a smooth seeded velocity field and pressure bumps to the current slot."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = sim.grid
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    fluid = sim.fluid[sim.cur].reshape(nz, ny, nx, 4).astype(np.float64)
+    e = fluid[..., 0]
+    for c in (1, 2, 3):
+        kx, ky, kz = rng.integers(1, 3, size=3)
+        ph = rng.uniform(0, 2 * np.pi)
+        fluid[..., c] += amp * e * np.sin(2 * np.pi * (kx * x / nx + ky * y / ny + kz * z / nz) + ph)
+    fluid[..., 0] *= 1.0 + 0.3 * amp * np.cos(2 * np.pi * (x / nx + 2 * y / ny)) ** 2
+    # a sharp jump so the limiter and HLL see a shock
+    fluid[nz // 2:, :, : nx // 3, 0] *= 1.5
+    sim.fluid[sim.cur] = fluid.reshape(-1, 4).astype(sim.dtype)
+
+
+CASES = [
+    # name, grid, bubbles (centre mode, radius), steps, velocity amplitude, seed
+    ("odd", (9, 11, 13), 3.5, 12, 0.30, 1),
+    ("tile_partial", (40, 20, 18), 6.0, 10, 0.20, 2),
+    ("flat", (64, 8, 8), 5.0, 8, 0.45, 3),
+]
+
+
+def make_cases() -> dict:
+    arrays = {}
+    for name, grid, r, steps, amp, seed in CASES:
+        for prec in ("f32", "f64"):
+            sched = oracle.make_schedule("centre", 1, r, grid, 10.0, 1)
+            sim = oracle.OracleSim(grid, schedule=sched, precision=prec)
+            sim.record_nucleation()
+            perturbed_state(sim, seed, amp)
+            f0, u0 = sim.state()
+            sim.advance(steps)
+            f1, u1 = sim.state()
+            arrays[f"{name}_{prec}_field0"] = f0
+            arrays[f"{name}_{prec}_fluid0"] = u0
+            arrays[f"{name}_{prec}_field"] = f1
+            arrays[f"{name}_{prec}_fluid"] = u1
+        arrays[f"{name}_grid"] = np.array(grid)
+        arrays[f"{name}_steps"] = np.array(steps)
+    return arrays
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--skip-128", action="store_true")
+    a = ap.parse_args()
+    oracle.build()
+    pub = parse_tables(Path(a.reference) / "docs" / "NUMERICS.md")
+    (HERE / "published_numerics.json").write_text(json.dumps(pub, indent=1))
+    np.savez_compressed(HERE / "cases.npz", **make_cases())
+    if not a.skip_128:
+        grid = (128, 128, 128)
+        d = oracle.derived(oracle.DEFAULT_MODEL)
+        sched = oracle.make_schedule("simultaneous", 1, d["seed_radius"], grid, 60.0, 1)
+        sim = oracle.OracleSim(grid, schedule=sched)
+        t0 = time.time()
+        sim.advance(100)
+        diag = sim.diagnostics()
+        out = {"case": "128^3, 1 bubble, simultaneous, seed 1, eta 0.3, cfl 0.2 (FP32 oracle)",
+               "seconds": time.time() - t0, "threads": oracle.lib().oracle_threads(),
+               "schedule": [[float(e[0]), [float(p) for p in e[1]], float(e[2])] for e in sched],
+               "oracle_step_100": {k: float(v) for k, v in diag.items()},
+               "published": pub["single_bubble"]}
+        (HERE / "single_bubble_128.json").write_text(json.dumps(out, indent=1))
+        print(json.dumps(out["oracle_step_100"], indent=1), out["seconds"])
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
