@@ -3,7 +3,9 @@
 
 #include <cuda_runtime.h>
 
-#include <atomic>
+#include <mutex>
+#include <utility>
+#include <vector>
 
 #include "kernels.cuh"
 #include "launch.h"
@@ -22,18 +24,25 @@ inline int grid_for(uint64_t n, int threads) {
     return (int)blocks;
 }
 
-// cudaFuncSetAttribute once per device and kernel instantiation.
-template <typename Kernel>
-inline cudaError_t ensure_smem(Kernel k, size_t bytes) {
-    static std::atomic<uint64_t> done_mask{0};
+// cudaFuncSetAttribute once per (kernel, device), keyed on the kernel's
+// address: every instantiation of a kernel template shares one function
+// type, so the key must be the function itself.
+inline cudaError_t ensure_smem_ptr(const void *k, size_t bytes) {
+    static std::mutex mu;
+    static std::vector<std::pair<const void *, int>> done;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    const uint64_t bit = 1ull << (dev & 63);
-    if (done_mask.load(std::memory_order_acquire) & bit) return cudaSuccess;
+    std::lock_guard<std::mutex> g(mu);
+    for (const auto &d : done)
+        if (d.first == k && d.second == dev) return cudaSuccess;
     e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e == cudaSuccess) done_mask.fetch_or(bit, std::memory_order_acq_rel);
+    if (e == cudaSuccess) done.emplace_back(k, dev);
     return e;
+}
+template <typename Kernel>
+inline cudaError_t ensure_smem(Kernel k, size_t bytes) {
+    return ensure_smem_ptr(reinterpret_cast<const void *>(k), bytes);
 }
 
 template <typename R>

@@ -280,12 +280,13 @@ def _sim_params(dtype, m: dict, grid, time=0.0) -> np.ndarray:
         buf[:3] = grid
         buf[4:] = np.array(fields, dtype=np.float32).view(np.uint32)
         return buf
-    buf = np.zeros(24, dtype=np.float64)
+    # FP64 instance: four u32 (16 bytes) then twenty doubles = 22 doubles
+    buf = np.zeros(22, dtype=np.float64)
     head = np.zeros(2, dtype=np.uint64)
     h32 = head.view(np.uint32)
     h32[:3] = grid
     buf[:2] = head.view(np.float64)
-    buf[4:] = np.array([float(x) for x in fields], dtype=np.float64)
+    buf[2:] = np.array([float(x) for x in fields], dtype=np.float64)
     return buf
 
 

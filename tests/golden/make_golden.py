@@ -4,7 +4,8 @@
 
 Writes into tests/golden/:
   published_numerics.json  the reference's published single-bubble and
-                           quiescent tables, parsed from its docs/NUMERICS.md
+                           quiescent tables (its docs/NUMERICS.md) and the
+                           grow/collapse threshold table (its docs/PHYSICS.md)
   single_bubble_128.json   the oracle's diagnostics of that published case
                            (128^3, 1 bubble, simultaneous, seed 1) at step 100,
                            beside the published row
@@ -46,6 +47,22 @@ def parse_tables(numerics_md: Path) -> dict:
         p = line.split()
         out["quiescent"][p[0]] = dict(broken_pct=float(p[1].rstrip("%")), max_v=float(p[2]), k=float(p[3]))
     return out
+
+
+def parse_threshold(physics_md: Path) -> dict:
+    """The grow/collapse table of docs/PHYSICS.md: broken % after 700 steps."""
+    text = physics_md.read_text()
+    t = {}
+    for line in text.splitlines():
+        m = re.match(r"\|\s*(0\.\d+)\s*\|\s*[\d.]+\s*\|\s*[\d.]+\s*\|(.*)\|\s*$", line)
+        if not m:
+            continue
+        cells = [c.strip() for c in m.group(2).split("|")]
+        if len(cells) != 4:
+            continue
+        for sf, c in zip(("0.90", "0.96", "1.00", "1.15"), cells):
+            t[f"{m.group(1)}_{sf}"] = None if c == "collapsed" else float(c.rstrip("%"))
+    return t
 
 
 def perturbed_state(sim: "oracle.OracleSim", seed: int, amp: float) -> None:
@@ -100,6 +117,7 @@ def main() -> int:
     a = ap.parse_args()
     oracle.build()
     pub = parse_tables(Path(a.reference) / "docs" / "NUMERICS.md")
+    pub["threshold_700"] = parse_threshold(Path(a.reference) / "docs" / "PHYSICS.md")
     (HERE / "published_numerics.json").write_text(json.dumps(pub, indent=1))
     np.savez_compressed(HERE / "cases.npz", **make_cases())
     if not a.skip_128:

@@ -116,6 +116,24 @@ def test_rk3_convex(oracle_mod):
 # src/gpu/sim.rs:1070-1078 parameter_blocks_have_the_expected_size
 def test_sim_params_size(oracle_mod):
     assert oracle_mod.lib().oracle_params_size_f32() == 96
+    m = oracle_mod.DEFAULT_MODEL
+    assert oracle_mod._sim_params(np.float32, m, (8, 8, 8)).nbytes == 96
+    assert oracle_mod._sim_params(np.float64, m, (8, 8, 8)).nbytes == oracle_mod.lib().oracle_params_size_f64()
+
+
+def test_fp64_oracle_tracks_fp32_oracle(oracle_mod):
+    """The two instances solve the same problem: they differ by rounding only."""
+    grid = (20, 16, 12)
+    sched = oracle_mod.make_schedule("centre", 1, 5.0, grid, 1.0, 1)
+    out = []
+    for prec in ("f32", "f64"):
+        sim = oracle_mod.OracleSim(grid, schedule=sched, precision=prec)
+        sim.advance(30)
+        out.append(sim.state())
+    for a, b in zip(out[0], out[1]):
+        scale = np.max(np.abs(b), axis=0)
+        assert np.max(np.max(np.abs(a - b), axis=0) / scale) < 1e-4
+    assert np.max(np.abs(out[1][0][:, 0])) > 0.3  # the (collapsing) bubble is still there
 
 
 def test_oracle_tanh_is_accurate(oracle_mod):
