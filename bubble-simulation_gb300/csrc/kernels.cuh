@@ -533,7 +533,8 @@ __global__ void __launch_bounds__(kDiagThreads)
         acc[2] += (double)kinetic;
         acc[3] += (double)e_lab;
         const float vl = (float)sqrt(v2);
-        if (!isfinite(e_total) || !isfinite(vl)) bad = 1;
+        // max(E, e_floor) hides a NaN in E, so the raw state is checked too.
+        if (!isfinite(e_total) || !isfinite(vl) || !isfinite(f.x + f.y + u.x + u.y + u.z + u.w)) bad = 1;
         vmaxv = fmaxf(vmaxv, vl);
     }
     __shared__ double sh[kDiagThreads / 32][4];
