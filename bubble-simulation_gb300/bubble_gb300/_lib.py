@@ -127,6 +127,7 @@ SIGNATURES = [
     ("bubble_ext_stream", _P, [_P]),
     ("bubble_ext_launches", ctypes.c_uint64, [_P]),
     ("bubble_ext_inject_allocation_failure", None, []),
+    ("bubble_diagnostics_noalloc", ctypes.c_int, [_P, _P, _U32P, ctypes.POINTER(Model), ctypes.c_int32, _P, _P]),
 ]
 
 _lib = None

@@ -52,6 +52,7 @@ KERNEL_UNITS = {
     "kernels_strict.cu": ["--fmad=false"],
     "kernels_fast.cu": ["--fmad=true"],
     "kernels_f64.cu": ["--fmad=false"],
+    "diag_noalloc.cu": ["--fmad=false"],
 }
 HOST_UNITS = ["physics.cpp", "simulation.cpp", "capi.cpp"]
 CLI_UNITS = ["headless.cpp"]

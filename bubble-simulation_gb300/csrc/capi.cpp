@@ -34,6 +34,10 @@ int done(int code, const std::string &msg) {
     } while (0)
 }  // namespace
 
+namespace bubble {
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+}  // namespace bubble
+
 extern "C" {
 
 const char *bubble_version(void) { return "bubble-gb300 0.1.0"; }

@@ -59,6 +59,9 @@ SimParamsHost sim_params(const bubble_model &m, const uint32_t grid[3]);
 // RK3 (src/gpu/sim.rs:133-135).
 extern const float kRK3[3][2];
 
+// Sets the message returned by bubble_last_error() on this thread.
+void set_last_error(const std::string &msg);
+
 // stage_slots (src/gpu/sim.rs:1046-1051).
 inline void stage_slots(uint32_t cur, uint32_t in[3], uint32_t out[3]) {
     const uint32_t a = cur % 3, b = (cur + 1) % 3, c = (cur + 2) % 3;

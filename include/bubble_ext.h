@@ -37,6 +37,41 @@ uint64_t bubble_ext_launches(const bubble_sim *sim);
  * injection for the failure-handling tests). */
 void bubble_ext_inject_allocation_failure(void);
 
+/* Raw FP64 result of the diagnostics reduction: sums over cells of the
+ * total energy density, broken-phase indicator, fluid kinetic energy
+ * density and fluid energy E; the bits of max|v| (a non-negative float);
+ * a non-zero `nonfinite` when any term or state value was not finite; the
+ * cell count. */
+typedef struct bubble_diag_raw {
+    double sums[4];
+    uint32_t max_v_bits;
+    uint32_t nonfinite;
+    uint64_t cells;
+} bubble_diag_raw;
+
+/* The diagnostics reduction of bubble_diagnostics for a caller that cannot
+ * allocate device memory.  No counterpart in the reference, whose
+ * reduction always runs on buffers the Simulation allocated itself.
+ *
+ * For engines that own all device memory through their own pool, real-time
+ * loops that must not allocate mid-run, or hosts with a fixed memory
+ * budget: the caller passes its own device buffers -- `field` (2 values per
+ * cell) and `fluid` (4 per cell), float for BUBBLE_PRECISION_SINGLE/MIXED,
+ * double for BUBBLE_PRECISION_DOUBLE, in the lattice order of this header --
+ * and a device pointer `result` to one bubble_diag_raw; the launch goes on
+ * `stream` (a cudaStream_t, NULL for the default stream) and is
+ * asynchronous.  The call allocates nothing: its scratch (1024 block
+ * partials and a completion counter, 49,408 bytes) is a static device array
+ * of the library, held on every GPU that loads the library until exit.
+ * Any lattice with axes 8..2048 fits; other sizes are rejected with
+ * BUBBLE_ERR_INVALID.  The first call on a device looks up the scratch
+ * address and loads the module there: make it before any stream capture.
+ * All calls share the scratch: the counter is cleared on `stream` before
+ * each launch, and calls that overlap on the GPU race. */
+int bubble_diagnostics_noalloc(const void *field, const void *fluid, const uint32_t grid[3],
+                               const bubble_model *model, int32_t precision, void *result,
+                               void *stream);
+
 #ifdef __cplusplus
 }
 #endif
