@@ -191,7 +191,8 @@ class Simulation:
         check(self._L.bubble_set_stream(self._h, stream_ptr))
 
     def set_path(self, path: str):
-        check(self._L.bubble_ext_set_path(self._h, _lib.PATH_REFERENCE if path == "reference" else _lib.PATH_FUSED))
+        """"fused" (default), "reference" (primitives + stage passes) or "fused_sync"."""
+        check(self._L.bubble_ext_set_path(self._h, _lib.PATHS[path]))
 
     def set_tile(self, ty: int, lz: int):
         check(self._L.bubble_ext_set_tile(self._h, ty, lz))

@@ -29,6 +29,8 @@ PRECISION = {"single": 0, "mixed": 1, "double": 2}
 MATH = {"fast": 0, "strict": 1}
 PATH_FUSED = 0
 PATH_REFERENCE = 1
+PATH_FUSED_SYNC = 2
+PATHS = {"fused": PATH_FUSED, "reference": PATH_REFERENCE, "fused_sync": PATH_FUSED_SYNC}
 MIN_GRID = 8
 MAX_GRID = 2048
 MAX_BATCH = 1024

@@ -53,3 +53,24 @@ int fused_threads(int ty) { return 32 * (ty + 1); }
 
 }  // namespace launch
 }  // namespace bubble
+
+namespace bubble {
+namespace launch {
+
+bool v2_shape_supported(int precision_double, int ty) {
+    return precision_double ? ty == 4 : (ty == 4 || ty == 8);
+}
+size_t v2_smem_bytes(int precision_double, int ty) {
+    if (precision_double) return dev::V2Layout<double, 4>::bytes;
+    return ty == 4 ? dev::V2Layout<float, 4>::bytes : dev::V2Layout<float, 8>::bytes;
+}
+cudaError_t stage_v2_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
+                                bool mixed, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
+    using namespace launch_detail;
+    if (shape.tx != 32 || shape.ty != 8) return cudaErrorInvalidValue;
+    if (mixed) return stage_v2<float, false, true, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+    return stage_v2<float, false, false, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+}
+
+}  // namespace launch
+}  // namespace bubble

@@ -11,6 +11,7 @@
 #include <cstdint>
 
 #include "params.h"
+#include "tma.h"
 
 namespace bubble {
 namespace launch {
@@ -61,6 +62,18 @@ cudaError_t diag_f64(const V2<double> *field, const V4<double> *fluid,
 // Scratch of the diagnostics reduction: partials + ticket.
 size_t diag_partials_bytes();
 int diag_blocks_for(uint64_t cells);
+
+// ---- fused stage kernel with asynchronous (TMA / cp.async) staging --------
+// `maps` are the tensor maps of the stage input slot (tma.h); `tma_ok` says
+// whether they are valid; bit 0 of *status is set if a bounded wait expired.
+bool v2_shape_supported(int precision_double, int ty);
+size_t v2_smem_bytes(int precision_double, int ty);
+cudaError_t stage_v2_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
+                                bool mixed, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
+cudaError_t stage_v2_f32_fast(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
+                              bool mixed, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
+cudaError_t stage_v2_f64(const StageArgs<double> &A, const LatticeParams<double> &P, TileShape shape,
+                         const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
 
 }  // namespace launch
 }  // namespace bubble

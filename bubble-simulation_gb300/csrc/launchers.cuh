@@ -9,6 +9,7 @@
 
 #include "kernels.cuh"
 #include "launch.h"
+#include "stage_v2.cuh"
 
 namespace bubble {
 namespace launch_detail {
@@ -94,6 +95,21 @@ cudaError_t stage_fused(const StageArgs<R> &A, const LatticeParams<R> &P, int lz
     const int nzc = (P.nz + lz - 1) / lz;
     dim3 grid(ntx * nty, nzc);
     k<<<grid, L::NT, L::bytes, s>>>(A, P, lz);
+    return cudaGetLastError();
+}
+
+template <typename R, bool FAST, bool MIXED, int TY>
+cudaError_t stage_v2(const StageArgs<R> &A, const LatticeParams<R> &P, int lz, const StageMaps &maps, int tma_ok,
+                     int *status, cudaStream_t s) {
+    using L = dev::V2Layout<R, TY>;
+    auto k = dev::stage_v2_kernel<R, FAST, MIXED, TY>;
+    cudaError_t e = ensure_smem(k, L::bytes);
+    if (e != cudaSuccess) return e;
+    if (lz < 1) lz = 1;
+    const int ntx = (P.nx + L::TX - 1) / L::TX, nty = (P.ny + TY - 1) / TY;
+    const int nzc = (P.nz + lz - 1) / lz;
+    dim3 grid(ntx * nty, nzc);
+    k<<<grid, L::NT, L::bytes, s>>>(A, P, lz, maps, tma_ok, status);
     return cudaGetLastError();
 }
 

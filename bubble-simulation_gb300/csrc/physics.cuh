@@ -84,12 +84,19 @@ BUBBLE_DEV R dpotential(R phi, const LatticeParams<R> &P) {
 // the sign), and then sign(a) * min(|a|, |b|, |c|) is that sign applied to
 // the minimum; every other case returns zero.  Same values, fewer
 // instructions.
-template <typename R>
+template <typename R, bool FAST = false>
 BUBBLE_DEV R limit_slope(R dm, R dp) {
-    const bool same = (dm > R(0) && dp > R(0)) || (dm < R(0) && dp < R(0));
-    const R a = fabs(R(0.5) * (dm + dp));
-    const R m = vmin(a, vmin(fabs(R(2.0) * dm), fabs(R(2.0) * dp)));
-    return same ? copysign(m, dm) : R(0);
+    if constexpr (FAST) {
+        // Same limiter with the sign test folded into one product (differs
+        // only when dm*dp underflows, i.e. for slopes below 1e-19).
+        const R m = vmin(fabs(R(0.5) * (dm + dp)), R(2.0) * vmin(fabs(dm), fabs(dp)));
+        return dm * dp > R(0) ? copysign(m, dm) : R(0);
+    } else {
+        const bool same = (dm > R(0) && dp > R(0)) || (dm < R(0) && dp < R(0));
+        const R a = fabs(R(0.5) * (dm + dp));
+        const R m = vmin(a, vmin(fabs(R(2.0) * dm), fabs(R(2.0) * dp)));
+        return same ? copysign(m, dm) : R(0);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -186,10 +193,10 @@ BUBBLE_DEV V4<R> v4_sub(const V4<R> &a, const V4<R> &b) {
 }
 
 // limit_slope4 (shaders/common.wgsl:129-136).
-template <typename R>
+template <typename R, bool FAST = false>
 BUBBLE_DEV V4<R> limit_slope4(const V4<R> &dm, const V4<R> &dp) {
-    return V4<R>{limit_slope(dm.x, dp.x), limit_slope(dm.y, dp.y), limit_slope(dm.z, dp.z),
-                 limit_slope(dm.w, dp.w)};
+    return V4<R>{limit_slope<R, FAST>(dm.x, dp.x), limit_slope<R, FAST>(dm.y, dp.y),
+                 limit_slope<R, FAST>(dm.z, dp.z), limit_slope<R, FAST>(dm.w, dp.w)};
 }
 
 // q + 0.5 s and q - 0.5 s (shaders/step.wgsl:135-144).
@@ -226,16 +233,24 @@ BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2) {
     const R v2 = vmin(vx * vx + vy * vy + vz * vz, zmax2);
     const R cs2 = R(1.0) / R(3.0);  // eos_sound_speed2 (eos.wgsl:50-53)
     if constexpr (FAST) {
-        const R w = R(4.0) * p * rcp_approx(R(1.0) - v2);
+        // 1 - vd^2 - cs2 (v^2 - vd^2) = 1 - (2/3) vd^2 - v^2/3 for cs2 = 1/3;
+        // E + p = w W^2, so the energy flux is w vd.
+        const R om = R(1.0) - v2;
+        const R w = (R(4.0) * p) * rcp_approx(om);
         s.u = V4<R>{w - p, w * vx, w * vy, w * vz};
         const R inv_den = rcp_approx(R(1.0) - v2 * cs2);
-        const R vd2 = vd * vd;
-        const R rad = vmax((R(1.0) - v2) * (R(1.0) - vd2 - cs2 * (v2 - vd2)), R(0.0));
-        const R a = vd * (R(1.0) - cs2) * inv_den;
+        const R tt = R(1.0) - (R(2.0) / R(3.0)) * (vd * vd) - cs2 * v2;
+        const R rad = vmax(om * tt, R(0.0));
         const R cs = R(0.57735026918962576451);
+        const R a = vd * ((R(2.0) / R(3.0)) * inv_den);
         const R b = cs * sqrt_approx(rad) * inv_den;
         s.lm = a - b;
         s.lp = a + b;
+        s.f = V4<R>{w * vd, s.u.y * vd, s.u.z * vd, s.u.w * vd};
+        if constexpr (AXIS == 0) s.f.y = s.f.y + p;
+        if constexpr (AXIS == 1) s.f.z = s.f.z + p;
+        if constexpr (AXIS == 2) s.f.w = s.f.w + p;
+        return s;
     } else {
         const R w = R(4.0) * p / (R(1.0) - v2);
         s.u = V4<R>{w - p, w * vx, w * vy, w * vz};

@@ -127,6 +127,8 @@ void Simulation::release() {
     partials_ = nullptr;
     ticket_ = nullptr;
     d_result_ = nullptr;
+    d_status_ = nullptr;
+    tma_ok_ = false;
     device_bytes_ = 0;
 }
 
@@ -159,7 +161,7 @@ int Simulation::allocate(std::string &err) {
         fluid_[k] = static_cast<char *>(state_) + k * slot + round_up(fb);
     }
     const size_t pb = round_up(launch::diag_partials_bytes());
-    const size_t scratch = pb + 256 + round_up(sizeof(DiagResult));
+    const size_t scratch = pb + 256 + round_up(sizeof(DiagResult)) + 256;
     e = device_alloc(&scratch_, scratch);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -170,7 +172,12 @@ int Simulation::allocate(std::string &err) {
     partials_ = scratch_;
     ticket_ = reinterpret_cast<unsigned int *>(static_cast<char *>(scratch_) + pb);
     d_result_ = reinterpret_cast<DiagResult *>(static_cast<char *>(scratch_) + pb + 256);
+    d_status_ = reinterpret_cast<int *>(static_cast<char *>(scratch_) + pb + 256 + round_up(sizeof(DiagResult)));
     BUBBLE_CUDA(cudaMemsetAsync(scratch_, 0, scratch, stream_), "cudaMemset");
+    tma_ok_ = true;
+    for (int k = 0; k < 3; ++k)
+        tma_ok_ = tma_ok_ && encode_stage_maps(&maps_[k], field_[k], fluid_[k], (int)grid_[0], (int)grid_[1],
+                                               (int)grid_[2], 32, tile_.ty, is_f64() ? 8 : 4);
     if (!h_result_) BUBBLE_CUDA(cudaMallocHost(reinterpret_cast<void **>(&h_result_), sizeof(DiagResult)), "cudaMallocHost");
     device_bytes_ = 3 * slot + scratch;
     return BUBBLE_OK;
@@ -276,11 +283,34 @@ int Simulation::resize(const uint32_t grid[3], std::string &err) {
 }
 
 int Simulation::set_tile(TileShape t, std::string &err) {
-    if (t.tx != 32 || !launch::fused_shape_supported(is_f64(), t.ty) || t.lz < 1) {
+    const bool strict = !is_f64() && spec_.math == BUBBLE_MATH_STRICT;
+    if (t.tx != 32 || !launch::fused_shape_supported(is_f64(), t.ty) || !launch::v2_shape_supported(is_f64(), t.ty) ||
+        (strict && t.ty != 8) || t.lz < 1) {
         err = "unsupported tile shape";
         return BUBBLE_ERR_INVALID;
     }
+    if (t.ty != tile_.ty) {
+        BUBBLE_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+        tma_ok_ = true;
+        for (int k = 0; k < 3; ++k)
+            tma_ok_ = tma_ok_ && encode_stage_maps(&maps_[k], field_[k], fluid_[k], (int)grid_[0], (int)grid_[1],
+                                                   (int)grid_[2], 32, t.ty, is_f64() ? 8 : 4);
+    }
     tile_ = t;
+    return BUBBLE_OK;
+}
+
+// A stage kernel whose bounded wait expired sets bit 0 of the status word;
+// it is read and cleared here after the stream has drained.
+int Simulation::check_status(std::string &err) {
+    int st = 0;
+    BUBBLE_CUDA(cudaMemcpyAsync(&st, d_status_, sizeof(int), cudaMemcpyDeviceToHost, stream_), "status readback");
+    BUBBLE_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    if (st != 0) {
+        BUBBLE_CUDA(cudaMemsetAsync(d_status_, 0, sizeof(int), stream_), "cudaMemset");
+        err = "a stage kernel gave up waiting for its staged data (status " + std::to_string(st) + ")";
+        return BUBBLE_ERR_TIMEOUT;
+    }
     return BUBBLE_OK;
 }
 
@@ -343,8 +373,11 @@ int Simulation::stage_launch(int stage, uint32_t in_slot, uint32_t out_slot, std
             e = launch::prim_f64(A.fluid_in, (V4<double> *)prim_, n, P, stream_);
             if (e == cudaSuccess) e = launch::stage_ref_f64(A, (const V4<double> *)prim_, P, stream_);
             launches_ += 2;
-        } else {
+        } else if (path_ == KernelPath::FusedSync) {
             e = launch::stage_fused_f64(A, P, tile_, stream_);
+            launches_ += 1;
+        } else {
+            e = launch::stage_v2_f64(A, P, tile_, maps_[in_slot], tma_ok_ ? 1 : 0, d_status_, stream_);
             launches_ += 1;
         }
     } else {
@@ -364,11 +397,16 @@ int Simulation::stage_launch(int stage, uint32_t in_slot, uint32_t out_slot, std
             e = launch::prim_f32(A.fluid_in, (V4<float> *)prim_, n, P, stream_);
             if (e == cudaSuccess) e = launch::stage_ref_f32(A, (const V4<float> *)prim_, P, stream_);
             launches_ += 2;
-        } else if (spec_.math == BUBBLE_MATH_STRICT) {
-            e = launch::stage_fused_f32_strict(A, P, tile_, mixed, stream_);
+        } else if (path_ == KernelPath::FusedSync) {
+            if (spec_.math == BUBBLE_MATH_STRICT) e = launch::stage_fused_f32_strict(A, P, tile_, mixed, stream_);
+            else e = launch::stage_fused_f32_fast(A, P, tile_, mixed, stream_);
             launches_ += 1;
         } else {
-            e = launch::stage_fused_f32_fast(A, P, tile_, mixed, stream_);
+            const int tma = tma_ok_ ? 1 : 0;
+            if (spec_.math == BUBBLE_MATH_STRICT)
+                e = launch::stage_v2_f32_strict(A, P, tile_, mixed, maps_[in_slot], tma, d_status_, stream_);
+            else
+                e = launch::stage_v2_f32_fast(A, P, tile_, mixed, maps_[in_slot], tma, d_status_, stream_);
             launches_ += 1;
         }
     }
@@ -436,6 +474,10 @@ int Simulation::diagnostics(bubble_diag *out, std::string &err) {
     BUBBLE_CUDA(cudaMemcpyAsync(h_result_, d_result_, sizeof(DiagResult), cudaMemcpyDeviceToHost, stream_),
                 "diagnostics readback");
     BUBBLE_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    {
+        const int rc = check_status(err);
+        if (rc != BUBBLE_OK) return rc;
+    }
     const DiagResult &r = *h_result_;
     // Diagnostics (src/gpu/sim.rs:991-1010): sums / cells.
     const float inv_n = 1.0f / (float)n_cells_;
@@ -479,6 +521,10 @@ int Simulation::nucleate_now(uint64_t rng_seed, std::string &err) {
 
 int Simulation::synchronize(std::string &err) {
     BUBBLE_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    {
+        const int rc = check_status(err);
+        if (rc != BUBBLE_OK) return rc;
+    }
     return BUBBLE_OK;
 }
 

@@ -19,13 +19,15 @@
 #include "../../include/bubble.h"
 #include "params.h"
 #include "physics.h"
+#include "tma.h"
 
 namespace bubble {
 
 // Which stage kernels to run.
 enum class KernelPath : int {
-    Fused = 0,      // one fused launch per RK stage (default)
+    Fused = 0,      // one fused launch per RK stage with async staging (default)
     Reference = 1,  // primitives pass + stage pass per RK stage, as in the reference
+    FusedSync = 2,  // the fused kernel with synchronous plane staging
 };
 
 class Simulation {
@@ -102,12 +104,16 @@ class Simulation {
     void *field_[3] = {nullptr, nullptr, nullptr};
     void *fluid_[3] = {nullptr, nullptr, nullptr};
     void *prim_ = nullptr;      // reference path only
-    void *scratch_ = nullptr;   // diag partials | ticket | result
+    void *scratch_ = nullptr;   // diag partials | ticket | result | status
     void *partials_ = nullptr;
     unsigned int *ticket_ = nullptr;
     DiagResult *d_result_ = nullptr;
+    int *d_status_ = nullptr;   // bit 0: a bounded wait in a stage kernel expired
     DiagResult *h_result_ = nullptr;  // pinned
     uint64_t device_bytes_ = 0;
+    StageMaps maps_[3];         // TMA maps of each slot as a stage input
+    bool tma_ok_ = false;
+    int check_status(std::string &err);
 
     cudaStream_t stream_ = nullptr;
     bool own_stream_ = false;

@@ -1,0 +1,447 @@
+// Fused SSP-RK3 stage kernel with asynchronous plane staging.
+//
+// Same arithmetic as stage_fused_kernel (shaders/primitives.wgsl +
+// shaders/step.wgsl:92-174, each face flux computed once), reorganised so
+// that no thread waits on a global load inside the z-march:
+//
+//   * Raw planes of U_in are staged into shared memory one iteration ahead.
+//     Tiles whose halo lies inside the lattice use the Tensor Memory
+//     Accelerator (cp.async.bulk.tensor, completion on an mbarrier); tiles
+//     on the periodic boundary, and lattices whose row pitch TMA cannot
+//     address, use per-element cp.async with wrapped addresses.
+//   * The own-cell U_in and U^n needed by the stage combine are loaded into
+//     registers one phase before they are used.
+//   * Two barriers per plane.  Phase X(z) combines plane z-1 and computes
+//     the limited face states of plane z; phase Y(z) recovers primitives of
+//     plane z+3 from the staged raw plane and computes the face fluxes of
+//     plane z.
+//
+// Every mbarrier wait is bounded by a clock limit; on expiry the CTA sets
+// bit 0 of *status, waits (bounded) for its own copy in flight and returns.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kernels.cuh"
+#include "tma.h"
+
+namespace bubble {
+namespace dev {
+
+BUBBLE_DEV uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+BUBBLE_DEV void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+BUBBLE_DEV void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+BUBBLE_DEV void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+BUBBLE_DEV void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+BUBBLE_DEV bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: ~2^31 SM cycles (about a second at GB300 clocks).
+BUBBLE_DEV bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+    const long long start = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - start > (1ll << 31)) return false;
+    }
+    return true;
+}
+BUBBLE_DEV void tma_load_4d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1, int c2, int c3) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(bar))
+        : "memory");
+}
+BUBBLE_DEV void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1, int c2) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(bar))
+        : "memory");
+}
+BUBBLE_DEV void cp_async_16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+BUBBLE_DEV void cp_async_8(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+BUBBLE_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+BUBBLE_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+template <typename R>
+BUBBLE_DEV void cp_async_v4(V4<R> *dst, const V4<R> *src) {
+    if constexpr (sizeof(R) == 4) {
+        cp_async_16(dst, src);
+    } else {
+        cp_async_16(dst, src);
+        cp_async_16(reinterpret_cast<char *>(dst) + 16, reinterpret_cast<const char *>(src) + 16);
+    }
+}
+template <typename R>
+BUBBLE_DEV void cp_async_v2(V2<R> *dst, const V2<R> *src) {
+    if constexpr (sizeof(R) == 4) cp_async_8(dst, src);
+    else cp_async_16(dst, src);
+}
+
+constexpr int pad32(int n) { return (n + 31) / 32 * 32; }
+constexpr size_t align128(size_t b) { return (b + 127) / 128 * 128; }
+
+template <typename R, int TY>
+struct V2Layout {
+    static constexpr int TX = 32;
+    static constexpr int PW = TX + 4, PH = TY + 4, PC = PW * PH, NC = TX * TY;
+    static constexpr int NT = TY == 8 ? 320 : 192;
+    static constexpr int MIN_BLOCKS = sizeof(R) == 4 ? 2 : 1;
+    // phase X: combine of the previous plane, then face states
+    static constexpr int X_C = NC, X_Z = NC, X_Y = TX * (TY + 2), X_X = (TX + 2) * TY;
+    static constexpr int X_TOTAL = X_C + X_Z + X_Y + X_X;
+    // phase Y: primitives of the staged plane, then face fluxes
+    static constexpr int A_REAL = TY * PW + 4 * TX;
+    static constexpr int Y_A = pad32(A_REAL), Y_Z = NC, Y_Y = TX * (TY + 1), Y_X = (TX + 1) * TY;
+    static constexpr int Y_TOTAL = Y_A + Y_Z + Y_Y + Y_X;
+    static constexpr int PRIM_RING = 4, PHI_RING = 5;
+    // shared memory map (bytes)
+    static constexpr size_t o_rawu = 0;
+    static constexpr size_t o_rawf = align128(o_rawu + 2 * PC * sizeof(V4<R>));
+    static constexpr size_t o_prim = align128(o_rawf + 2 * PC * sizeof(V2<R>));
+    static constexpr size_t o_phi = align128(o_prim + PRIM_RING * PC * sizeof(V4<R>));
+    static constexpr size_t o_xlo = align128(o_phi + PHI_RING * PC * sizeof(R));
+    static constexpr size_t o_xhi = o_xlo + TY * (TX + 2) * sizeof(V4<R>);
+    static constexpr size_t o_ylo = o_xhi + TY * (TX + 2) * sizeof(V4<R>);
+    static constexpr size_t o_yhi = o_ylo + (TY + 2) * TX * sizeof(V4<R>);
+    static constexpr size_t o_zlo = o_yhi + (TY + 2) * TX * sizeof(V4<R>);
+    static constexpr size_t o_zhi = o_zlo + NC * sizeof(V4<R>);
+    static constexpr size_t o_fx = o_zhi + 2 * NC * sizeof(V4<R>);
+    static constexpr size_t o_fy = o_fx + TY * (TX + 1) * sizeof(V4<R>);
+    static constexpr size_t o_fz = o_fy + (TY + 1) * TX * sizeof(V4<R>);
+    static constexpr size_t o_bar = o_fz + 2 * NC * sizeof(V4<R>);
+    static constexpr size_t bytes = o_bar + 2 * sizeof(uint64_t);
+    static constexpr uint32_t plane_tx_bytes = PC * (sizeof(V4<R>) + sizeof(V2<R>));
+    static_assert(NT >= NC, "the combine phase maps one thread per column");
+    static_assert(X_C % 32 == 0 && (X_C + X_Z) % 32 == 0 && (X_C + X_Z + X_Y) % 32 == 0, "warp-uniform X");
+    static_assert(Y_A % 32 == 0 && (Y_A + Y_Z) % 32 == 0 && (Y_A + Y_Z + Y_Y) % 32 == 0, "warp-uniform Y");
+};
+
+// Cross-shaped halo item k of a plane -> smem (i, j).
+template <int TX, int TY, int PW>
+BUBBLE_DEV void cross_item(int k, int &i, int &j) {
+    constexpr int band = TY * PW;
+    if (k < band) {
+        j = 2 + k / PW;
+        i = k - (j - 2) * PW;
+    } else {
+        const int kk = k - band;
+        const int r = kk / TX;
+        j = r < 2 ? r : TY + r;
+        i = 2 + (kk - r * TX);
+    }
+}
+
+template <typename R, bool FAST, bool MIXED, int TY>
+__global__ void __launch_bounds__(V2Layout<R, TY>::NT, V2Layout<R, TY>::MIN_BLOCKS)
+    stage_v2_kernel(StageArgs<R> A, LatticeParams<R> P, int lz, const __grid_constant__ StageMaps maps,
+                    int tma_ok, int *status) {
+    using L = V2Layout<R, TY>;
+    constexpr int TX = L::TX, NT = L::NT, PW = L::PW, PC = L::PC, NC = L::NC;
+    extern __shared__ __align__(128) unsigned char smem[];
+    V4<R> *raw_u = reinterpret_cast<V4<R> *>(smem + L::o_rawu);
+    V2<R> *raw_f = reinterpret_cast<V2<R> *>(smem + L::o_rawf);
+    V4<R> *prim_s = reinterpret_cast<V4<R> *>(smem + L::o_prim);
+    R *phi_s = reinterpret_cast<R *>(smem + L::o_phi);
+    V4<R> *xlo = reinterpret_cast<V4<R> *>(smem + L::o_xlo);
+    V4<R> *xhi = reinterpret_cast<V4<R> *>(smem + L::o_xhi);
+    V4<R> *ylo = reinterpret_cast<V4<R> *>(smem + L::o_ylo);
+    V4<R> *yhi = reinterpret_cast<V4<R> *>(smem + L::o_yhi);
+    V4<R> *zlo = reinterpret_cast<V4<R> *>(smem + L::o_zlo);
+    V4<R> *zhi = reinterpret_cast<V4<R> *>(smem + L::o_zhi);
+    V4<R> *fxs = reinterpret_cast<V4<R> *>(smem + L::o_fx);
+    V4<R> *fys = reinterpret_cast<V4<R> *>(smem + L::o_fy);
+    V4<R> *fzs = reinterpret_cast<V4<R> *>(smem + L::o_fz);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::o_bar);
+
+    const int t = threadIdx.x;
+    const int ntx = (P.nx + TX - 1) / TX;
+    const int x0 = (blockIdx.x % ntx) * TX;
+    const int y0 = (blockIdx.x / ntx) * TY;
+    const int z0 = blockIdx.y * lz;
+    const int z1 = min(z0 + lz, P.nz);
+    const int xe = min(TX, P.nx - x0);
+    const int ye = min(TY, P.ny - y0);
+    const R zmax2 = P.z_max * P.z_max;
+    const size_t plane = (size_t)P.nx * (size_t)P.ny;
+    const bool tma = tma_ok && x0 >= 2 && x0 + TX + 2 <= P.nx && y0 >= 2 && y0 + TY + 2 <= P.ny;
+    const int zlast = z1 + 1;  // last plane whose primitives are needed
+
+    auto prim_slot = [&](int p) { return prim_s + ((p + 8) & (L::PRIM_RING - 1)) * PC; };
+    auto phi_slot = [&](int p) { return phi_s + ((p + 10) % L::PHI_RING) * PC; };
+    auto raw_slot = [&](int p) { return (p - (z0 + 3)) & 1; };
+
+    if (tma && t == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+
+    // Stage raw plane p (p >= z0+3) asynchronously.
+    auto issue = [&](int p) {
+        const int s = raw_slot(p);
+        const int gz = wrap1(p, P.nz);
+        if (tma) {
+            if (t == 0) {
+                fence_proxy_async();
+                mbar_expect_tx(&bar[s], L::plane_tx_bytes);
+                tma_load_4d(raw_u + s * PC, &maps.fluid, &bar[s], 0, x0 - 2, y0 - 2, gz);
+                tma_load_3d(raw_f + s * PC, &maps.field, &bar[s], 2 * (x0 - 2), y0 - 2, gz);
+            }
+        } else {
+            const size_t base = (size_t)gz * plane;
+            for (int k = t; k < L::A_REAL; k += NT) {
+                int i, j;
+                cross_item<TX, TY, PW>(k, i, j);
+                if (i >= xe + 4 || j >= ye + 4) continue;
+                const int gx = wrap1(x0 - 2 + i, P.nx);
+                const int gy = wrap1(y0 - 2 + j, P.ny);
+                const size_t g = base + (size_t)gy * P.nx + gx;
+                cp_async_v4(raw_u + s * PC + j * PW + i, A.fluid_in + g);
+                cp_async_v2(raw_f + s * PC + j * PW + i, A.field_in + g);
+            }
+            cp_async_commit();
+        }
+    };
+    // Wait for raw plane p; returns false when the bounded wait expired.
+    auto wait_plane = [&](int p) -> bool {
+        if (tma) {
+            const uint32_t parity = ((p - (z0 + 3)) >> 1) & 1;
+            return mbar_wait_bounded(&bar[raw_slot(p)], parity);
+        }
+        cp_async_wait_all();
+        return true;
+    };
+
+    // Synchronous staging used by the prologue (planes z0-2 .. z0+2).
+    auto stage_plane_sync = [&](int p) {
+        const int gz = wrap1(p, P.nz);
+        const size_t base = (size_t)gz * plane;
+        V4<R> *pr = prim_slot(p);
+        R *ph = phi_slot(p);
+        for (int k = t; k < L::A_REAL; k += NT) {
+            int i, j;
+            cross_item<TX, TY, PW>(k, i, j);
+            if (i >= xe + 4 || j >= ye + 4) continue;
+            const int gx = wrap1(x0 - 2 + i, P.nx);
+            const int gy = wrap1(y0 - 2 + j, P.ny);
+            const size_t g = base + (size_t)gy * P.nx + gx;
+            const V4<R> u = A.fluid_in[g];
+            ph[j * PW + i] = A.field_in[g].x;
+            pr[j * PW + i] = sanitise(recover<R, FAST, MIXED>(u, P), P.p_floor, zmax2);
+        }
+    };
+    auto z_states = [&](int p, int n, V4<R> &lo, V4<R> &hi) {
+        const int i = n % TX, j = n / TX;
+        const int c = (j + 2) * PW + (i + 2);
+        const V4<R> q = prim_slot(p)[c];
+        const V4<R> s = limit_slope4<R, FAST>(v4_sub(q, prim_slot(p - 1)[c]), v4_sub(prim_slot(p + 1)[c], q));
+        lo = sanitise(half_step(q, s, R(-1)), P.p_floor, zmax2);
+        hi = sanitise(half_step(q, s, R(1)), P.p_floor, zmax2);
+    };
+
+    // ---- prologue ----------------------------------------------------------
+    // Planes z0-2 .. z0+1 fill the 4-slot primitive ring; the z face
+    // z0 - 1/2 needs all four.  Plane z0+2 then takes the slot of z0-2.
+    for (int p = z0 - 2; p <= z0 + 1; ++p) stage_plane_sync(p);
+    __syncthreads();  // also publishes the mbarrier initialisation
+    for (int n = t; n < NC; n += NT) {
+        V4<R> lo_m, hi_m, lo_0, hi_0;
+        z_states(z0 - 1, n, lo_m, hi_m);
+        z_states(z0, n, lo_0, hi_0);
+        zhi[((z0 + 8) & 1) * NC + n] = hi_0;
+        fzs[((z0 - 1 + 8) & 1) * NC + n] = hll_flux<2, R, FAST>(hi_m, lo_0, zmax2);
+    }
+    __syncthreads();
+    stage_plane_sync(z0 + 2);
+    if (z0 + 3 <= zlast) issue(z0 + 3);
+    __syncthreads();
+
+    // own-cell state of the plane awaiting its combine, loaded a phase ahead
+    V2<R> pf{R(0), R(0)}, pfn{R(0), R(0)};
+    V4<R> pu{R(0), R(0), R(0), R(0)}, pun{R(0), R(0), R(0), R(0)};
+
+    for (int z = z0;; ++z) {
+        // ---- phase X(z): combine plane z-1, face states of plane z --------
+        for (int k = t; k < L::X_TOTAL; k += NT) {
+            if (k < L::X_C) {
+                if (z == z0) continue;
+                const int zc = z - 1;
+                const int i = k % TX, j = k / TX;
+                if (i >= xe || j >= ye) continue;
+                const int c = (j + 2) * PW + (i + 2);
+                const R *ph0 = phi_slot(zc);
+                const R *phm = phi_slot(zc - 1);
+                const R *php = phi_slot(zc + 1);
+                const R phi0 = ph0[c], pi0 = pf.y;
+                const V4<R> q0 = prim_slot(zc)[c];
+                R lap_sum = R(0), gx, gy, gz;
+                {
+                    const R m = ph0[c - 1], p = ph0[c + 1];
+                    lap_sum = lap_sum + (m + p - R(2.0) * phi0);
+                    gx = R(0.5) * (p - m) * P.inv_dx;
+                }
+                {
+                    const R m = ph0[c - PW], p = ph0[c + PW];
+                    lap_sum = lap_sum + (m + p - R(2.0) * phi0);
+                    gy = R(0.5) * (p - m) * P.inv_dx;
+                }
+                {
+                    const R m = phm[c], p = php[c];
+                    lap_sum = lap_sum + (m + p - R(2.0) * phi0);
+                    gz = R(0.5) * (p - m) * P.inv_dx;
+                }
+                const V4<R> fxm = fxs[j * (TX + 1) + i], fxp = fxs[j * (TX + 1) + i + 1];
+                const V4<R> fym = fys[j * TX + i], fyp = fys[(j + 1) * TX + i];
+                const V4<R> fzm = fzs[((zc - 1 + 8) & 1) * NC + k], fzp = fzs[((zc + 8) & 1) * NC + k];
+                V4<R> fd;
+                if constexpr (FAST) {
+                    fd.x = ((fxp.x - fxm.x) + (fyp.x - fym.x) + (fzp.x - fzm.x)) * P.inv_dx;
+                    fd.y = ((fxp.y - fxm.y) + (fyp.y - fym.y) + (fzp.y - fzm.y)) * P.inv_dx;
+                    fd.z = ((fxp.z - fxm.z) + (fyp.z - fym.z) + (fzp.z - fzm.z)) * P.inv_dx;
+                    fd.w = ((fxp.w - fxm.w) + (fyp.w - fym.w) + (fzp.w - fzm.w)) * P.inv_dx;
+                } else {
+                    fd = V4<R>{R(0), R(0), R(0), R(0)};
+                    fd.x = fd.x + (fxp.x - fxm.x) * P.inv_dx;
+                    fd.y = fd.y + (fxp.y - fxm.y) * P.inv_dx;
+                    fd.z = fd.z + (fxp.z - fxm.z) * P.inv_dx;
+                    fd.w = fd.w + (fxp.w - fxm.w) * P.inv_dx;
+                    fd.x = fd.x + (fyp.x - fym.x) * P.inv_dx;
+                    fd.y = fd.y + (fyp.y - fym.y) * P.inv_dx;
+                    fd.z = fd.z + (fyp.z - fym.z) * P.inv_dx;
+                    fd.w = fd.w + (fyp.w - fym.w) * P.inv_dx;
+                    fd.x = fd.x + (fzp.x - fzm.x) * P.inv_dx;
+                    fd.y = fd.y + (fzp.y - fzm.y) * P.inv_dx;
+                    fd.z = fd.z + (fzp.z - fzm.z) * P.inv_dx;
+                    fd.w = fd.w + (fzp.w - fzm.w) * P.inv_dx;
+                }
+                const R laplacian = lap_sum * P.inv_dx * P.inv_dx;
+                const R vv = q0.x * q0.x + q0.y * q0.y + q0.z * q0.z;
+                R gam;
+                if constexpr (FAST) gam = rsqrt_approx(vmax(R(1.0) - vv, R(1e-12)));
+                else gam = R(1.0) / sqrt(vmax(R(1.0) - vv, R(1e-12)));
+                const R drag = P.eta * (gam * (pi0 + (q0.x * gx + q0.y * gy + q0.z * gz)));
+                const R d_pi = laplacian - dpotential(phi0, P) - drag;
+                const R dE = -fd.x + drag * pi0;
+                const R dZx = -fd.y - drag * gx;
+                const R dZy = -fd.z - drag * gy;
+                const R dZz = -fd.w - drag * gz;
+                const V2<R> fu{pf.x + A.dt * pi0, pf.y + A.dt * d_pi};
+                const V4<R> uu{pu.x + A.dt * dE, pu.y + A.dt * dZx, pu.z + A.dt * dZy, pu.w + A.dt * dZz};
+                const size_t g = (size_t)zc * plane + (size_t)(y0 + j) * P.nx + (x0 + i);
+                if (A.stage == 0) {
+                    A.field_out[g] = V2<R>{A.a1 * fu.x, A.a1 * fu.y};
+                    A.fluid_out[g] = V4<R>{A.a1 * uu.x, A.a1 * uu.y, A.a1 * uu.z, A.a1 * uu.w};
+                } else {
+                    A.field_out[g] = V2<R>{A.a0 * pfn.x + A.a1 * fu.x, A.a0 * pfn.y + A.a1 * fu.y};
+                    A.fluid_out[g] = V4<R>{A.a0 * pun.x + A.a1 * uu.x, A.a0 * pun.y + A.a1 * uu.y,
+                                           A.a0 * pun.z + A.a1 * uu.z, A.a0 * pun.w + A.a1 * uu.w};
+                }
+            } else if (z < z1) {
+                const int kk = k - L::X_C;
+                if (kk < L::X_Z) {
+                    V4<R> lo, hi;
+                    z_states(z + 1, kk, lo, hi);
+                    zlo[kk] = lo;
+                    zhi[((z + 1 + 8) & 1) * NC + kk] = hi;
+                } else if (kk < L::X_Z + L::X_Y) {
+                    const int q = kk - L::X_Z;
+                    const int jj = q / TX;  // cell row jj-1
+                    const int i = q - jj * TX;
+                    const int c = (jj + 1) * PW + (i + 2);
+                    const V4<R> *pr = prim_slot(z);
+                    const V4<R> qc = pr[c];
+                    const V4<R> s = limit_slope4<R, FAST>(v4_sub(qc, pr[c - PW]), v4_sub(pr[c + PW], qc));
+                    ylo[jj * TX + i] = sanitise(half_step(qc, s, R(-1)), P.p_floor, zmax2);
+                    yhi[jj * TX + i] = sanitise(half_step(qc, s, R(1)), P.p_floor, zmax2);
+                } else {
+                    const int q = kk - L::X_Z - L::X_Y;
+                    const int j = q / (TX + 2);
+                    const int ii = q - j * (TX + 2);  // cell column ii-1
+                    const int c = (j + 2) * PW + (ii + 1);
+                    const V4<R> *pr = prim_slot(z);
+                    const V4<R> qc = pr[c];
+                    const V4<R> s = limit_slope4<R, FAST>(v4_sub(qc, pr[c - 1]), v4_sub(pr[c + 1], qc));
+                    xlo[j * (TX + 2) + ii] = sanitise(half_step(qc, s, R(-1)), P.p_floor, zmax2);
+                    xhi[j * (TX + 2) + ii] = sanitise(half_step(qc, s, R(1)), P.p_floor, zmax2);
+                }
+            }
+        }
+        if (z == z1) break;
+        bool timed_out = false;
+        if (z + 3 <= zlast) timed_out = !wait_plane(z + 3);
+        if (__syncthreads_or(timed_out)) {
+            if (t == 0) atomicOr(status, 1);
+            if (tma) wait_plane(z + 3);  // bounded: drain the copy in flight
+            return;
+        }
+        // ---- phase Y(z): stage the next plane, primitives of z+3, fluxes ---
+        if (z + 4 <= zlast) issue(z + 4);
+        if (t < NC) {
+            const int i = t % TX, j = t / TX;
+            if (i < xe && j < ye) {
+                const size_t g = (size_t)z * plane + (size_t)(y0 + j) * P.nx + (x0 + i);
+                pf = A.field_in[g];
+                pu = A.fluid_in[g];
+                if (A.stage != 0) {
+                    pfn = A.field_n[g];
+                    pun = A.fluid_n[g];
+                }
+            }
+        }
+        const bool do_a = z + 3 <= zlast;
+        for (int k = t; k < L::Y_TOTAL; k += NT) {
+            if (k < L::Y_A) {
+                if (!do_a || k >= L::A_REAL) continue;
+                int i, j;
+                cross_item<TX, TY, PW>(k, i, j);
+                if (i >= xe + 4 || j >= ye + 4) continue;
+                const int s = raw_slot(z + 3);
+                const int c = j * PW + i;
+                const V4<R> u = raw_u[s * PC + c];
+                phi_slot(z + 3)[c] = raw_f[s * PC + c].x;
+                prim_slot(z + 3)[c] = sanitise(recover<R, FAST, MIXED>(u, P), P.p_floor, zmax2);
+            } else {
+                const int kk = k - L::Y_A;
+                if (kk < L::Y_Z) {
+                    fzs[((z + 8) & 1) * NC + kk] = hll_flux<2, R, FAST>(zhi[((z + 8) & 1) * NC + kk], zlo[kk], zmax2);
+                } else if (kk < L::Y_Z + L::Y_Y) {
+                    const int q = kk - L::Y_Z;
+                    const int f = q / TX;  // face between rows f-1 and f
+                    const int i = q - f * TX;
+                    fys[f * TX + i] = hll_flux<1, R, FAST>(yhi[f * TX + i], ylo[(f + 1) * TX + i], zmax2);
+                } else {
+                    const int q = kk - L::Y_Z - L::Y_Y;
+                    const int j = q / (TX + 1);
+                    const int f = q - j * (TX + 1);  // face between columns f-1 and f
+                    fxs[j * (TX + 1) + f] =
+                        hll_flux<0, R, FAST>(xhi[j * (TX + 2) + f], xlo[j * (TX + 2) + f + 1], zmax2);
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace dev
+}  // namespace bubble

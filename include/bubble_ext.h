@@ -19,6 +19,8 @@ extern "C" {
 #define BUBBLE_PATH_FUSED 0     /* one fused launch per stage (default)       */
 #define BUBBLE_PATH_REFERENCE 1 /* primitives pass + stage pass per stage,
                                    the reference's own kernel structure      */
+#define BUBBLE_PATH_FUSED_SYNC 2 /* the fused kernel staging planes with
+                                    synchronous loads (for comparison)       */
 int bubble_ext_set_path(bubble_sim *sim, int32_t path);
 
 /* Tile of the fused kernel: y extent (4 or 8 for FP32, 4 for FP64; x is 32)
