@@ -58,6 +58,11 @@ def workload(name: str) -> dict:
         return dict(name="128^3 periodic, 12 bubbles, nucleation times uniform over the first 200 steps, "
                          "eta 0.3, FP32", grid=(128, 128, 128), bubbles=12, nucleation="uniform",
                     duration=40.0, eta=0.3, precision="single", seed=1)
+    if name == "profile256":
+        return dict(name="256^3 periodic, 32 bubbles at t=0 (1.15 R_c), eta 0.3, FP32 state + FP64 "
+                         "reductions + FP64 con2prim where gamma>3 (small case of precision512 for ncu)",
+                    grid=(256, 256, 256), bubbles=32, nucleation="simultaneous", duration=1.0, eta=0.3,
+                    precision="mixed", seed=1)
     if name == "plain64":
         return dict(name="64^3 periodic, 1 bubble at the centre (1.15 R_c), eta 0.3, FP32",
                     grid=(64, 64, 64), bubbles=1, nucleation="centre", duration=1.0, eta=0.3,
@@ -77,7 +82,7 @@ def peaks() -> tuple[float, str]:
 
 def ncu_traffic(wl: str) -> float | None:
     """DRAM bytes per cell per stage launch from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "stage_fused_traffic.txt"
+    p = ROOT / "profiles" / "stage_v2_traffic.txt"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -324,7 +329,7 @@ def main() -> int:
                 "frac": achieved / peak, "peak_kind": peak_kind,
                 "traffic": (traffic_per_cell * cells / 3) if traffic_per_cell else None,
                 "algorithmic_bytes_per_launch": BYTES_PER_CELL_UPDATE * cells / 3,
-                "kernel": "stage_fused_kernel (3 launches per step)"}
+                "kernel": "stage_v2_kernel (3 launches per step)"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

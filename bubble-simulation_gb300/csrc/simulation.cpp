@@ -52,9 +52,11 @@ int default_chunk(const uint32_t grid[3], int ty) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long tiles = (long)((grid[0] + 31) / 32) * (long)((grid[1] + ty - 1) / ty);
-    // Aim at >= 8 CTAs per SM over the launch while keeping chunks >= 16
-    // planes so the 4-plane warm-up stays below a quarter of the work.
-    const long want = (long)sms * 8;
+    // Aim at >= 24 CTAs per SM over the launch (about a dozen waves of two
+    // resident CTAs, so the tail wave is short) while keeping chunks >= 16
+    // planes so the 5-plane prologue stays below a third of the work.
+    // Measured at 512^3: lz = 128 beats 256 by 3 % and 64 by 1 %.
+    const long want = (long)sms * 24;
     long chunks = (want + tiles - 1) / tiles;
     if (chunks < 1) chunks = 1;
     long lz = ((long)grid[2] + chunks - 1) / chunks;
