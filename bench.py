@@ -230,6 +230,74 @@ def run_reference(args, wl: dict, world: int, rank: int) -> int:
     return 0
 
 
+def batch_specs(bubble, n: int, seed: int = 20251203):
+    """The batched-ensemble workload: n lattices, edges drawn from {32, 48, 64, 96},
+    one bubble at the centre, seed factor U[0.7, 1.5], eta log-U[0.02, 1]."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for k in range(n):
+        edge = int(rng.choice([32, 48, 64, 96]))
+        model = bubble.Model(eta=float(math.exp(rng.uniform(math.log(0.02), math.log(1.0)))),
+                             seed_value=float(rng.uniform(0.7, 1.5)))
+        specs.append(bubble.SimulationSpec(model=model, grid=(edge,) * 3, nucleation="centre", bubbles=1,
+                                           seed=k + 1, math="fast"))
+    return specs
+
+
+def run_batch(args) -> int:
+    """Batched ensemble (solves/s): one persistent graph-captured launch per
+    chunk of steps for all lattices, against the same plain kernels run one
+    lattice at a time (each with its autotuned z chunk)."""
+    import torch
+    import bubble_gb300 as bubble
+
+    bubble.load()
+    n, steps = args.lattices, args.batch_steps
+    specs = batch_specs(bubble, n)
+    cells = sum(s.grid[0] ** 3 for s in specs)
+    t0 = time.perf_counter()
+    b = bubble.Batch(specs)
+    setup_s = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    chunk = 100
+    done = 0
+    while done < steps:
+        b.advance(min(chunk, steps - done))
+        done += min(chunk, steps - done)
+    broken_b = [b.diagnostics(k).broken_fraction for k in range(n)]
+    t_batch = time.perf_counter() - t0
+    info = b.info()
+    b.close()
+    lz_cache = {}
+    t_plain = 0.0
+    broken_p = []
+    for s in specs:
+        if s.grid not in lz_cache:
+            lz_cache[s.grid] = bubble.autotune_chunk(s.grid, 8, "fast")
+        sim = bubble.Simulation(s)
+        sim.set_tile(8, lz_cache[s.grid])
+        sim.synchronize()
+        t0 = time.perf_counter()
+        sim.advance(steps)
+        d = sim.diagnostics()
+        t_plain += time.perf_counter() - t0
+        broken_p.append(d.broken_fraction)
+        sim.close()
+    agree = sum((a > 0) == (p > 0) for a, p in zip(broken_b, broken_p))
+    line = {"metric": "solves/s", "value": n / t_batch, "unit": "solves/s", "n_gpus": 1, "steps": steps,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic", "impl": "gb300-batch",
+            "config": {"workload": f"{n} lattices, edges from {{32,48,64,96}}, 1 bubble, seed factor U[0.7,1.5], "
+                                   f"eta log-U[0.02,1], {steps} steps, FP32 fast", "cells": cells},
+            "plain_solves_per_s": n / t_plain, "speedup_vs_plain": t_plain / t_batch,
+            "batch_cell_updates_per_s": cells * steps / t_batch,
+            "plain_cell_updates_per_s": cells * steps / t_plain,
+            "outcome_agreement": f"{agree}/{n}", "grown_batch": sum(x > 0 for x in broken_b),
+            "batch_info": info, "setup_s": setup_s}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -239,8 +307,12 @@ def main() -> int:
     ap.add_argument("--workload", default="precision512")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--lattices", type=int, default=64, help="batch64 workload: number of lattices")
+    ap.add_argument("--batch-steps", type=int, default=1000, help="batch64 workload: steps per solve")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.workload == "batch64":
+        return run_batch(args)
     wl = workload(args.workload)
     world, rank, local = dist_setup()
 

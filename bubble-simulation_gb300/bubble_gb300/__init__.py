@@ -280,3 +280,73 @@ class Simulation:
         fluid = np.ascontiguousarray(fluid, dtype=self._dtype).reshape(n, 4)
         fn = self._L.bubble_load_state_f64 if self._dtype == np.float64 else self._L.bubble_load_state
         check(fn(self._h, field.ctypes.data, fluid.ctypes.data))
+
+
+class Batch:
+    """Many independent lattices advanced by one persistent, graph-captured
+    launch per chunk of steps (include/bubble_batch.h)."""
+
+    def __init__(self, specs: list[SimulationSpec], tile_y: int = 8, autotune: bool = True,
+                 use_graph: bool = True, max_grid: int = 0):
+        self._L = load()
+        self.specs = list(specs)
+        arr = (_lib.Spec * len(specs))(*[s.c() for s in specs])
+        opt = _lib.BatchOptions(tile_y, int(autotune), int(use_graph), max_grid)
+        h = ctypes.c_void_p()
+        check(self._L.bubble_batch_create(arr, len(specs), ctypes.byref(opt), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.bubble_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __len__(self):
+        return len(self.specs)
+
+    def advance(self, n: int):
+        check(self._L.bubble_batch_advance(self._h, n))
+
+    def diagnostics(self, k: int) -> Diagnostics:
+        d = _lib.Diag()
+        check(self._L.bubble_batch_diagnostics(self._h, k, ctypes.byref(d)))
+        return Diagnostics(**{n: getattr(d, n) for n, _ in _lib.Diag._fields_})
+
+    def copy_state(self, k: int) -> tuple[np.ndarray, np.ndarray]:
+        g = self.specs[k].grid
+        n = g[0] * g[1] * g[2]
+        field = np.empty((n, 2), dtype=np.float32)
+        fluid = np.empty((n, 4), dtype=np.float32)
+        check(self._L.bubble_batch_copy_state(self._h, k, field.ctypes.data, fluid.ctypes.data))
+        return field, fluid
+
+    def load_state(self, k: int, field: np.ndarray, fluid: np.ndarray):
+        field = np.ascontiguousarray(field, dtype=np.float32)
+        fluid = np.ascontiguousarray(fluid, dtype=np.float32)
+        check(self._L.bubble_batch_load_state(self._h, k, field.ctypes.data, fluid.ctypes.data))
+
+    def time(self, k: int) -> float:
+        return self._L.bubble_batch_time(self._h, k)
+
+    def info(self) -> dict:
+        i = _lib.BatchInfo()
+        check(self._L.bubble_batch_info_get(self._h, ctypes.byref(i)))
+        return {n: getattr(i, n) for n, _ in _lib.BatchInfo._fields_}
+
+
+def autotune_chunk(grid, tile_y: int = 8, math: str = "fast") -> int:
+    lz = ctypes.c_int32()
+    check(load().bubble_autotune_chunk((ctypes.c_uint32 * 3)(*grid), tile_y, _lib.MATH[math], ctypes.byref(lz)))
+    return lz.value

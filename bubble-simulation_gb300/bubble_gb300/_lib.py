@@ -70,6 +70,17 @@ class Diag(ctypes.Structure):
                 ("cells", ctypes.c_uint64)]
 
 
+class BatchOptions(ctypes.Structure):
+    _fields_ = [("tile_y", ctypes.c_int32), ("autotune", ctypes.c_int32), ("use_graph", ctypes.c_int32),
+                ("max_grid", ctypes.c_int32)]
+
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("lattices", ctypes.c_uint32), ("grid", ctypes.c_uint32), ("items", ctypes.c_uint32),
+                ("tile_y", ctypes.c_int32), ("graph", ctypes.c_int32), ("autotuned", ctypes.c_int32),
+                ("cells", ctypes.c_uint64), ("launches", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64)]
+
+
 class VramInfo(ctypes.Structure):
     _fields_ = [("capacity", ctypes.c_uint64), ("budget", ctypes.c_uint64),
                 ("used", ctypes.c_uint64), ("has_budget", ctypes.c_int32)]
@@ -130,6 +141,18 @@ SIGNATURES = [
     ("bubble_ext_launches", ctypes.c_uint64, [_P]),
     ("bubble_ext_inject_allocation_failure", None, []),
     ("bubble_diagnostics_noalloc", ctypes.c_int, [_P, _P, _U32P, ctypes.POINTER(Model), ctypes.c_int32, _P, _P]),
+    # bubble_batch.h
+    ("bubble_batch_options_default", None, [ctypes.POINTER(BatchOptions)]),
+    ("bubble_batch_create", ctypes.c_int, [ctypes.POINTER(Spec), ctypes.c_uint32, ctypes.POINTER(BatchOptions),
+                                           ctypes.POINTER(_P)]),
+    ("bubble_batch_destroy", None, [_P]),
+    ("bubble_batch_advance", ctypes.c_int, [_P, ctypes.c_uint64]),
+    ("bubble_batch_diagnostics", ctypes.c_int, [_P, ctypes.c_uint32, ctypes.POINTER(Diag)]),
+    ("bubble_batch_copy_state", ctypes.c_int, [_P, ctypes.c_uint32, _P, _P]),
+    ("bubble_batch_load_state", ctypes.c_int, [_P, ctypes.c_uint32, _P, _P]),
+    ("bubble_batch_info_get", ctypes.c_int, [_P, ctypes.POINTER(BatchInfo)]),
+    ("bubble_batch_time", ctypes.c_float, [_P, ctypes.c_uint32]),
+    ("bubble_autotune_chunk", ctypes.c_int, [_U32P, ctypes.c_int32, ctypes.c_int32, _I32P]),
 ]
 
 _lib = None

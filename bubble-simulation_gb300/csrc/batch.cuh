@@ -1,0 +1,113 @@
+// Batched form: many independent lattices of uneven size advanced by one
+// persistent, cooperative launch.
+//
+// The launch runs `steps` SSP-RK3 steps of every lattice in the batch.  Each
+// RK stage is a list of work items -- (lattice, column tile, z chunk), the
+// unit of the fused stage kernel -- handed out dynamically from one atomic
+// counter, largest lattices first; a grid-wide barrier separates the stages
+// because a stage reads its neighbours' outputs of the previous one.  Every
+// lattice keeps its own slot rotation (src/gpu/sim.rs:1046-1051).  The grid
+// barrier's wait is bounded; on expiry bit 1 of *status is set and the CTA
+// leaves, so the others expire in turn at their next barrier.
+#pragma once
+
+#include "batch_desc.h"
+#include "stage_v2.cuh"
+
+namespace bubble {
+namespace dev {
+
+// Bounded grid barrier for a cooperative launch.  Returns false on expiry.
+BUBBLE_DEV bool grid_barrier(unsigned int *count, unsigned int *gen, int *status) {
+    __shared__ int ok_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int *vgen = gen;
+        const unsigned int g = *vgen;
+        // The next stage reads this stage's stores through TMA (the async
+        // proxy): order generic-proxy writes before async-proxy reads.
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+        __threadfence();
+        const unsigned int arrived = atomicAdd(count, 1u) + 1u;
+        int ok = 1;
+        if (arrived == gridDim.x) {
+            atomicExch(count, 0u);
+            __threadfence();
+            atomicAdd(gen, 1u);
+        } else {
+            const long long t0 = clock64();
+            while (*vgen == g) {
+                if (clock64() - t0 > (1ll << 32)) {
+                    ok = 0;
+                    atomicOr(status, 2);
+                    break;
+                }
+                __nanosleep(100);
+            }
+        }
+        __threadfence();
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+        ok_s = ok;
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+
+// sync: counters[0] = barrier count, counters[1] = barrier generation,
+//       counters[2] = work counter (zeroed before the launch).
+template <bool FAST, int TY>
+__global__ void __launch_bounds__(V2Layout<float, TY>::NT, V2Layout<float, TY>::MIN_BLOCKS)
+    batch_v2_kernel(const BatchLattice *__restrict__ lat, int n_lat, int n_items, int steps,
+                    unsigned int *counters, int *status) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ int item_s;
+    const float rk[3][2] = {{0.0f, 1.0f}, {0.75f, 0.25f}, {1.0f / 3.0f, 2.0f / 3.0f}};
+    unsigned int round = 0;
+    // Every CTA ends a round with one grab past the last item, so a round
+    // consumes exactly n_items + gridDim.x grabs of the counter.
+    const unsigned int per_round = (unsigned int)n_items + gridDim.x;
+    for (int step = 0; step < steps; ++step) {
+        for (int stage = 0; stage < 3; ++stage, ++round) {
+            const unsigned int base = round * per_round;
+            while (true) {
+                __syncthreads();
+                if (threadIdx.x == 0) item_s = (int)(atomicAdd(&counters[2], 1u) - base);
+                __syncthreads();
+                const int item = item_s;
+                if (item >= n_items) break;
+                // lattice of this item: largest item_begin <= item
+                int lo = 0, hi = n_lat - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (lat[mid].item_begin <= item) lo = mid;
+                    else hi = mid - 1;
+                }
+                const BatchLattice &B = lat[lo];
+                const int local = item - B.item_begin;
+                const int cur = (B.cur0 + step) % 3;
+                const int a = cur, b = (cur + 1) % 3, c = (cur + 2) % 3;
+                const int in_slot = stage == 0 ? a : (stage == 1 ? b : c);
+                const int out_slot = stage == 1 ? c : b;
+                StageArgs<float> A;
+                A.field_n = B.field[a];
+                A.fluid_n = B.fluid[a];
+                A.field_in = B.field[in_slot];
+                A.fluid_in = B.fluid[in_slot];
+                A.field_out = B.field[out_slot];
+                A.fluid_out = B.fluid[out_slot];
+                A.a0 = rk[stage][0];
+                A.a1 = rk[stage][1];
+                A.dt = B.dt;
+                A.stage = stage;
+                const LatticeParams<float> P = B.P;
+                if (!v2_item<float, FAST, false, TY>(smem, A, P, B.lz, &B.maps[in_slot], B.tma_ok, status,
+                                                     local % B.tiles_xy, local / B.tiles_xy))
+                    return;
+            }
+            if (!grid_barrier(&counters[0], &counters[1], status)) return;
+        }
+    }
+}
+
+}  // namespace dev
+}  // namespace bubble

@@ -44,3 +44,26 @@ cudaError_t stage_v2_f32_fast(const StageArgs<float> &A, const LatticeParams<flo
 
 }  // namespace launch
 }  // namespace bubble
+
+namespace bubble {
+namespace launch {
+
+int batch_max_grid(bool fast, int ty) {
+    if (!fast) return batch_max_grid_strict(ty);
+    if (ty == 8) return launch_detail::batch_max_grid<true, 8>();
+    if (ty == 4) return launch_detail::batch_max_grid<true, 4>();
+    return 0;
+}
+size_t batch_smem_bytes(int ty) {
+    return ty == 4 ? dev::V2Layout<float, 4>::bytes : dev::V2Layout<float, 8>::bytes;
+}
+cudaError_t batch_launch(bool fast, int ty, const void *lat, int n_lat, int n_items, int steps,
+                         unsigned int *counters, int *status, int grid, cudaStream_t s) {
+    if (!fast) return batch_launch_strict(ty, lat, n_lat, n_items, steps, counters, status, grid, s);
+    if (ty == 8) return launch_detail::batch_launch<true, 8>(lat, n_lat, n_items, steps, counters, status, grid, s);
+    if (ty == 4) return launch_detail::batch_launch<true, 4>(lat, n_lat, n_items, steps, counters, status, grid, s);
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace launch
+}  // namespace bubble

@@ -74,3 +74,19 @@ cudaError_t stage_v2_f32_strict(const StageArgs<float> &A, const LatticeParams<f
 
 }  // namespace launch
 }  // namespace bubble
+
+namespace bubble {
+namespace launch {
+
+int batch_max_grid_strict(int ty) {
+    if (ty != 8) return 0;
+    return launch_detail::batch_max_grid<false, 8>();
+}
+cudaError_t batch_launch_strict(int ty, const void *lat, int n_lat, int n_items, int steps,
+                                unsigned int *counters, int *status, int grid, cudaStream_t s) {
+    if (ty != 8) return cudaErrorInvalidValue;
+    return launch_detail::batch_launch<false, 8>(lat, n_lat, n_items, steps, counters, status, grid, s);
+}
+
+}  // namespace launch
+}  // namespace bubble

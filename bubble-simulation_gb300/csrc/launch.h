@@ -77,3 +77,27 @@ cudaError_t stage_v2_f64(const StageArgs<double> &A, const LatticeParams<double>
 
 }  // namespace launch
 }  // namespace bubble
+
+namespace bubble {
+namespace launch {
+
+// ---- batched persistent launch (batch.cuh) ---------------------------------
+// lat: device array of BatchLattice; counters: 3 zeroed uint32 (barrier
+// count, barrier generation, work counter).  Cooperative launch with `grid`
+// CTAs, which must not exceed batch_max_grid(fast, ty).
+int batch_max_grid(bool fast, int ty);
+size_t batch_smem_bytes(int ty);
+cudaError_t batch_launch(bool fast, int ty, const void *lat, int n_lat, int n_items, int steps,
+                         unsigned int *counters, int *status, int grid, cudaStream_t s);
+
+}  // namespace launch
+}  // namespace bubble
+
+namespace bubble {
+namespace launch {
+// strict-mode halves of the batch entry points (kernels_strict.cu)
+int batch_max_grid_strict(int ty);
+cudaError_t batch_launch_strict(int ty, const void *lat, int n_lat, int n_items, int steps,
+                                unsigned int *counters, int *status, int grid, cudaStream_t s);
+}  // namespace launch
+}  // namespace bubble

@@ -125,3 +125,36 @@ cudaError_t diag(const V2<R> *field, const V4<R> *fluid, const LatticeParams<R> 
 
 }  // namespace launch_detail
 }  // namespace bubble
+
+#include "batch.cuh"
+
+namespace bubble {
+namespace launch_detail {
+
+template <bool FAST, int TY>
+int batch_max_grid() {
+    using L = dev::V2Layout<float, TY>;
+    auto k = dev::batch_v2_kernel<FAST, TY>;
+    if (ensure_smem(k, L::bytes) != cudaSuccess) return 0;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, L::NT, L::bytes) != cudaSuccess) return 0;
+    return per_sm * sms;
+}
+
+template <bool FAST, int TY>
+cudaError_t batch_launch(const void *lat, int n_lat, int n_items, int steps, unsigned int *counters,
+                         int *status, int grid, cudaStream_t s) {
+    using L = dev::V2Layout<float, TY>;
+    auto k = dev::batch_v2_kernel<FAST, TY>;
+    cudaError_t e = ensure_smem(k, L::bytes);
+    if (e != cudaSuccess) return e;
+    const BatchLattice *lp = static_cast<const BatchLattice *>(lat);
+    void *args[] = {(void *)&lp, (void *)&n_lat, (void *)&n_items, (void *)&steps, (void *)&counters,
+                    (void *)&status};
+    return cudaLaunchCooperativeKernel((const void *)k, dim3(grid), dim3(L::NT), args, L::bytes, s);
+}
+
+}  // namespace launch_detail
+}  // namespace bubble

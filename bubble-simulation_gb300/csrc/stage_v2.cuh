@@ -152,13 +152,17 @@ BUBBLE_DEV void cross_item(int k, int &i, int &j) {
     }
 }
 
+// One work item: the column tile `tile_xy` of lattice P, z chunk `chunk`
+// (planes [chunk*lz, min((chunk+1)*lz, nz))), one RK stage.  Returns false
+// when a bounded wait expired (bit 0 of *status is set); the CTA must then
+// stop.  Usable repeatedly by one CTA: it starts with a barrier and leaves
+// no copy in flight.
 template <typename R, bool FAST, bool MIXED, int TY>
-__global__ void __launch_bounds__(V2Layout<R, TY>::NT, V2Layout<R, TY>::MIN_BLOCKS)
-    stage_v2_kernel(StageArgs<R> A, LatticeParams<R> P, int lz, const __grid_constant__ StageMaps maps,
-                    int tma_ok, int *status) {
+BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const LatticeParams<R> &P, int lz,
+                        const StageMaps *maps, int tma_ok, int *status, int tile_xy, int chunk) {
     using L = V2Layout<R, TY>;
     constexpr int TX = L::TX, NT = L::NT, PW = L::PW, PC = L::PC, NC = L::NC;
-    extern __shared__ __align__(128) unsigned char smem[];
+    __syncthreads();  // a previous item on this CTA is done with shared memory
     V4<R> *raw_u = reinterpret_cast<V4<R> *>(smem + L::o_rawu);
     V2<R> *raw_f = reinterpret_cast<V2<R> *>(smem + L::o_rawf);
     V4<R> *prim_s = reinterpret_cast<V4<R> *>(smem + L::o_prim);
@@ -176,9 +180,9 @@ __global__ void __launch_bounds__(V2Layout<R, TY>::NT, V2Layout<R, TY>::MIN_BLOC
 
     const int t = threadIdx.x;
     const int ntx = (P.nx + TX - 1) / TX;
-    const int x0 = (blockIdx.x % ntx) * TX;
-    const int y0 = (blockIdx.x / ntx) * TY;
-    const int z0 = blockIdx.y * lz;
+    const int x0 = (tile_xy % ntx) * TX;
+    const int y0 = (tile_xy / ntx) * TY;
+    const int z0 = chunk * lz;
     const int z1 = min(z0 + lz, P.nz);
     const int xe = min(TX, P.nx - x0);
     const int ye = min(TY, P.ny - y0);
@@ -205,8 +209,8 @@ __global__ void __launch_bounds__(V2Layout<R, TY>::NT, V2Layout<R, TY>::MIN_BLOC
             if (t == 0) {
                 fence_proxy_async();
                 mbar_expect_tx(&bar[s], L::plane_tx_bytes);
-                tma_load_4d(raw_u + s * PC, &maps.fluid, &bar[s], 0, x0 - 2, y0 - 2, gz);
-                tma_load_3d(raw_f + s * PC, &maps.field, &bar[s], 2 * (x0 - 2), y0 - 2, gz);
+                tma_load_4d(raw_u + s * PC, &maps->fluid, &bar[s], 0, x0 - 2, y0 - 2, gz);
+                tma_load_3d(raw_f + s * PC, &maps->field, &bar[s], 2 * (x0 - 2), y0 - 2, gz);
             }
         } else {
             const size_t base = (size_t)gz * plane;
@@ -393,7 +397,7 @@ __global__ void __launch_bounds__(V2Layout<R, TY>::NT, V2Layout<R, TY>::MIN_BLOC
         if (__syncthreads_or(timed_out)) {
             if (t == 0) atomicOr(status, 1);
             if (tma) wait_plane(z + 3);  // bounded: drain the copy in flight
-            return;
+            return false;
         }
         // ---- phase Y(z): stage the next plane, primitives of z+3, fluxes ---
         if (z + 4 <= zlast) issue(z + 4);
@@ -441,6 +445,15 @@ __global__ void __launch_bounds__(V2Layout<R, TY>::NT, V2Layout<R, TY>::MIN_BLOC
         }
         __syncthreads();
     }
+    return true;
+}
+
+template <typename R, bool FAST, bool MIXED, int TY>
+__global__ void __launch_bounds__(V2Layout<R, TY>::NT, V2Layout<R, TY>::MIN_BLOCKS)
+    stage_v2_kernel(StageArgs<R> A, LatticeParams<R> P, int lz, const __grid_constant__ StageMaps maps,
+                    int tma_ok, int *status) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    v2_item<R, FAST, MIXED, TY>(smem, A, P, lz, &maps, tma_ok, status, blockIdx.x, blockIdx.y);
 }
 
 }  // namespace dev
