@@ -298,6 +298,96 @@ def run_batch(args) -> int:
     return 0
 
 
+def serve_requests(bubble, n: int, seed: int = 20251203):
+    """The serving workload: edges from {48, 64, 128, 192, 256}, 1-32 bubbles
+    with nucleation times uniform over the first 200 steps, eta log-U[0.02, 1],
+    seed factor U[0.9, 1.5], 500-3000 steps; Poisson arrivals at 20 req/s."""
+    rng = np.random.default_rng(seed)
+    reqs, t = [], 0.0
+    for k in range(n):
+        t += float(rng.exponential(1.0 / 20.0))
+        edge = int(rng.choice([48, 64, 128, 192, 256]))
+        model = bubble.Model(eta=float(math.exp(rng.uniform(math.log(0.02), math.log(1.0)))),
+                             seed_value=float(rng.uniform(0.9, 1.5)))
+        spec = bubble.SimulationSpec(model=model, grid=(edge,) * 3, nucleation="uniform",
+                                     bubbles=int(rng.integers(1, 33)), nucleation_duration=40.0, seed=k + 1,
+                                     math="fast")
+        reqs.append((t, spec, int(rng.integers(500, 3001))))
+    return reqs
+
+
+def percentile(xs, p):
+    xs = sorted(xs)
+    pos = p * (len(xs) - 1)
+    i = int(math.floor(pos))
+    j = min(i + 1, len(xs) - 1)
+    return xs[i] + (pos - i) * (xs[j] - xs[i])
+
+
+def run_serve(args) -> int:
+    """Serving stream: requests arrive (Poisson, 20/s) while others run and join
+    the batched launch at the next round; latency = completion - arrival.  The
+    plain path answers the same requests one at a time in arrival order."""
+    import bubble_gb300 as bubble
+
+    bubble.load()
+    reqs = serve_requests(bubble, args.requests)
+    n = len(reqs)
+
+    def serve(policy):
+        srv = bubble.Server(math="fast", chunk_steps=50, policy=policy)
+        base = srv.now()
+        arrival_of, i, done = {}, 0, []
+        while len(done) < n:
+            now = srv.now() - base
+            while i < n and reqs[i][0] <= now:
+                rid = srv.submit(reqs[i][1], reqs[i][2])
+                arrival_of[rid] = base + reqs[i][0]
+                i += 1
+            busy = srv.tick()
+            done += srv.poll()
+            if not busy and i < n:
+                time.sleep(max(0.0, reqs[i][0] - (srv.now() - base)))
+        lat = [r["done_s"] - arrival_of[r["id"]] for r in done]
+        span = max(r["done_s"] for r in done) - (base + reqs[0][0])
+        st = srv.stats()
+        srv.close()
+        return lat, span, st
+
+    lat, span, st = serve("fifo")
+    lat_sj, span_sj, _ = serve("shortest")
+    # plain path: one request at a time, in arrival order
+    durations = []
+    for _, spec, steps in reqs:
+        sim = bubble.Simulation(spec)
+        sim.synchronize()
+        t0 = time.perf_counter()
+        sim.advance(steps)
+        sim.diagnostics()
+        durations.append(time.perf_counter() - t0)
+        sim.close()
+    free_at, plain_lat, finish = 0.0, [], 0.0
+    for (arr, _, _), d in zip(reqs, durations):
+        start = max(free_at, arr)
+        free_at = start + d
+        plain_lat.append(free_at - arr)
+        finish = free_at
+    cells = sum(s.grid[0] ** 3 * k for _, s, k in reqs)
+    line = {"metric": "solves/s", "value": n / span, "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic", "impl": "gb300-serve",
+            "config": {"workload": f"{n} requests, Poisson 20/s, edges from {{48,64,128,192,256}}, 1-32 bubbles, "
+                                   "eta log-U[0.02,1], seed factor U[0.9,1.5], 500-3000 steps, FP32 fast"},
+            "p50_latency_s": percentile(lat, 0.5), "p99_latency_s": percentile(lat, 0.99),
+            "cell_updates_per_s": cells / span, "policy": "fifo with backfill, 24 M resident cells",
+            "shortest_first": {"solves_per_s": n / span_sj, "p50_latency_s": percentile(lat_sj, 0.5),
+                               "p99_latency_s": percentile(lat_sj, 0.99)},
+            "plain": {"solves_per_s": n / (finish - reqs[0][0]), "p50_latency_s": percentile(plain_lat, 0.5),
+                      "p99_latency_s": percentile(plain_lat, 0.99), "cell_updates_per_s": cells / sum(durations)},
+            "server_stats": st}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -309,10 +399,13 @@ def main() -> int:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--lattices", type=int, default=64, help="batch64 workload: number of lattices")
     ap.add_argument("--batch-steps", type=int, default=1000, help="batch64 workload: steps per solve")
+    ap.add_argument("--requests", type=int, default=24, help="serve workload: number of requests")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.workload == "batch64":
         return run_batch(args)
+    if args.workload == "serve":
+        return run_serve(args)
     wl = workload(args.workload)
     world, rank, local = dist_setup()
 

@@ -350,3 +350,69 @@ def autotune_chunk(grid, tile_y: int = 8, math: str = "fast") -> int:
     lz = ctypes.c_int32()
     check(load().bubble_autotune_chunk((ctypes.c_uint32 * 3)(*grid), tile_y, _lib.MATH[math], ctypes.byref(lz)))
     return lz.value
+
+
+class Server:
+    """Request loop with continuous batching (include/bubble_server.h)."""
+
+    def __init__(self, math: str = "fast", chunk_steps: int = 50, max_active: int = 64,
+                 memory_fraction: float = 0.85, use_graph: bool = True, tile_y: int = 8,
+                 resident_cells: int = 0, policy: str = "fifo"):
+        self._L = load()
+        opt = _lib.ServerOptions(_lib.MATH[math], tile_y, chunk_steps, max_active, memory_fraction, int(use_graph),
+                                 resident_cells, _lib.SERVE_POLICY[policy])
+        h = ctypes.c_void_p()
+        check(self._L.bubble_server_create(ctypes.byref(opt), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.bubble_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, spec: SimulationSpec, steps: int) -> int:
+        i = ctypes.c_uint64()
+        check(self._L.bubble_server_submit(self._h, ctypes.byref(spec.c()), steps, ctypes.byref(i)))
+        return i.value
+
+    def tick(self) -> bool:
+        busy = ctypes.c_int32()
+        check(self._L.bubble_server_tick(self._h, ctypes.byref(busy)))
+        return bool(busy.value)
+
+    def run_until_idle(self):
+        check(self._L.bubble_server_run_until_idle(self._h))
+
+    def poll(self) -> list[dict]:
+        out = (_lib.ServerResult * 256)()
+        n = ctypes.c_uint64()
+        res = []
+        while True:
+            check(self._L.bubble_server_poll(self._h, out, 256, ctypes.byref(n)))
+            for k in range(n.value):
+                r = out[k]
+                res.append(dict(id=r.id, status=r.status, grid=tuple(r.grid), steps=r.steps, submit_s=r.submit_s,
+                                admit_s=r.admit_s, done_s=r.done_s,
+                                diag=Diagnostics(**{f: getattr(r.diag, f) for f, _ in _lib.Diag._fields_})))
+            if n.value < 256:
+                return res
+
+    def stats(self) -> dict:
+        s = _lib.ServerStats()
+        check(self._L.bubble_server_stats_get(self._h, ctypes.byref(s)))
+        return {n: getattr(s, n) for n, _ in _lib.ServerStats._fields_}
+
+    def now(self) -> float:
+        return self._L.bubble_server_now(self._h)

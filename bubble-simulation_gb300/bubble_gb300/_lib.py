@@ -81,6 +81,27 @@ class BatchInfo(ctypes.Structure):
                 ("cells", ctypes.c_uint64), ("launches", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64)]
 
 
+class ServerOptions(ctypes.Structure):
+    _fields_ = [("math", ctypes.c_int32), ("tile_y", ctypes.c_int32), ("chunk_steps", ctypes.c_uint32),
+                ("max_active", ctypes.c_uint32), ("memory_fraction", ctypes.c_float), ("use_graph", ctypes.c_int32),
+                ("resident_cells", ctypes.c_uint64), ("policy", ctypes.c_int32)]
+
+
+SERVE_POLICY = {"fifo": 0, "shortest": 1}
+
+
+class ServerResult(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_uint64), ("status", ctypes.c_int32), ("grid", ctypes.c_uint32 * 3),
+                ("steps", ctypes.c_uint64), ("submit_s", ctypes.c_double), ("admit_s", ctypes.c_double),
+                ("done_s", ctypes.c_double), ("diag", Diag)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "admitted", "completed", "queued", "active", "rounds")] + \
+               [(n, ctypes.c_double) for n in ("p50_latency_s", "p99_latency_s", "mean_latency_s", "solves_per_s",
+                                               "cell_updates")]
+
+
 class VramInfo(ctypes.Structure):
     _fields_ = [("capacity", ctypes.c_uint64), ("budget", ctypes.c_uint64),
                 ("used", ctypes.c_uint64), ("has_budget", ctypes.c_int32)]
@@ -153,6 +174,16 @@ SIGNATURES = [
     ("bubble_batch_info_get", ctypes.c_int, [_P, ctypes.POINTER(BatchInfo)]),
     ("bubble_batch_time", ctypes.c_float, [_P, ctypes.c_uint32]),
     ("bubble_autotune_chunk", ctypes.c_int, [_U32P, ctypes.c_int32, ctypes.c_int32, _I32P]),
+    # bubble_server.h
+    ("bubble_server_options_default", None, [ctypes.POINTER(ServerOptions)]),
+    ("bubble_server_create", ctypes.c_int, [ctypes.POINTER(ServerOptions), ctypes.POINTER(_P)]),
+    ("bubble_server_destroy", None, [_P]),
+    ("bubble_server_submit", ctypes.c_int, [_P, ctypes.POINTER(Spec), ctypes.c_uint64, _U64P]),
+    ("bubble_server_tick", ctypes.c_int, [_P, _I32P]),
+    ("bubble_server_run_until_idle", ctypes.c_int, [_P]),
+    ("bubble_server_poll", ctypes.c_int, [_P, ctypes.POINTER(ServerResult), ctypes.c_uint64, _U64P]),
+    ("bubble_server_stats_get", ctypes.c_int, [_P, ctypes.POINTER(ServerStats)]),
+    ("bubble_server_now", ctypes.c_double, [_P]),
 ]
 
 _lib = None

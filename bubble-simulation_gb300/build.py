@@ -54,7 +54,7 @@ KERNEL_UNITS = {
     "kernels_f64.cu": ["--fmad=false"],
     "diag_noalloc.cu": ["--fmad=false"],
 }
-HOST_UNITS = ["physics.cpp", "simulation.cpp", "capi.cpp", "tma.cpp", "batch.cpp", "capi_batch.cpp"]
+HOST_UNITS = ["physics.cpp", "simulation.cpp", "capi.cpp", "tma.cpp", "batch.cpp", "capi_batch.cpp", "server.cpp"]
 CLI_UNITS = ["headless.cpp"]
 HEADERS = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
 

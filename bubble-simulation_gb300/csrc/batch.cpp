@@ -49,6 +49,21 @@ LatticeParams<float> params_of(const bubble_model &m, const uint32_t grid[3]) {
 std::mutex g_tune_mu;
 std::map<std::tuple<uint32_t, uint32_t, uint32_t, int, bool>, int> g_tune_cache;
 
+constexpr size_t kOffStatus = 64;     // counters at 0 (16 B), status at 64
+constexpr size_t kOffDiag = 256;      // diag partials | ticket | result
+
+std::string check_spec(const bubble_spec &s, int math) {
+    const std::string msg = validate_model(s.model);
+    if (!msg.empty()) return msg;
+    if (s.precision != BUBBLE_PRECISION_SINGLE) return "a batch runs FP32 lattices (BUBBLE_PRECISION_SINGLE)";
+    if (s.math != math) return "all lattices of a batch share one math mode";
+    for (int a = 0; a < 3; ++a)
+        if (s.grid[a] < BUBBLE_MIN_GRID || s.grid[a] > BUBBLE_MAX_GRID) return "grid axis out of 8..2048";
+    if (s.nucleation < BUBBLE_NUCLEATION_SIMULTANEOUS || s.nucleation > BUBBLE_NUCLEATION_UNIFORM)
+        return "unknown nucleation mode";
+    return "";
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -113,49 +128,63 @@ int autotune_chunk(const uint32_t grid[3], int ty, bool fast, std::string &err) 
 // ---------------------------------------------------------------------------
 //  Batch
 // ---------------------------------------------------------------------------
-int Batch::create(const bubble_spec *specs, uint32_t n, const bubble_batch_options *opt,
-                  std::unique_ptr<Batch> &out, std::string &err) {
-    if (n == 0) {
-        err = "a batch needs at least one lattice";
-        return BUBBLE_ERR_INVALID;
-    }
+int Batch::setup(int math, const bubble_batch_options *opt, std::string &err) {
     bubble_batch_options o;
     o.tile_y = 8;
     o.autotune = 1;
     o.use_graph = 1;
     o.max_grid = 0;
     if (opt) o = *opt;
-    const int math = specs[0].math;
-    for (uint32_t k = 0; k < n; ++k) {
-        const std::string msg = validate_model(specs[k].model);
-        if (!msg.empty()) {
-            err = "lattice " + std::to_string(k) + ": " + msg;
-            return BUBBLE_ERR_INVALID;
-        }
-        if (specs[k].precision != BUBBLE_PRECISION_SINGLE) {
-            err = "a batch runs FP32 lattices (BUBBLE_PRECISION_SINGLE)";
-            return BUBBLE_ERR_INVALID;
-        }
-        if (specs[k].math != math) {
-            err = "all lattices of a batch share one math mode";
-            return BUBBLE_ERR_INVALID;
-        }
-        for (int a = 0; a < 3; ++a)
-            if (specs[k].grid[a] < BUBBLE_MIN_GRID || specs[k].grid[a] > BUBBLE_MAX_GRID) {
-                err = "lattice " + std::to_string(k) + ": grid axis out of 8..2048";
-                return BUBBLE_ERR_INVALID;
-            }
+    math_ = math;
+    fast_ = math == BUBBLE_MATH_FAST;
+    if (math != BUBBLE_MATH_FAST && math != BUBBLE_MATH_STRICT) {
+        err = "unknown math mode";
+        return BUBBLE_ERR_INVALID;
     }
-    const bool fast = math == BUBBLE_MATH_FAST;
-    if (o.tile_y != 8 && !(fast && o.tile_y == 4)) {
+    if (o.tile_y != 8 && !(fast_ && o.tile_y == 4)) {
         err = "batch tile_y must be 8 (or 4 in the fast mode)";
         return BUBBLE_ERR_INVALID;
     }
+    ty_ = o.tile_y;
+    use_graph_ = o.use_graph != 0;
+    autotuned_ = false;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
         err = "no CUDA device is available (this library has no CPU path)";
         return BUBBLE_ERR_CUDA;
+    }
+    BATCH_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    const size_t pb = (launch::diag_partials_bytes() + 255) & ~(size_t)255;
+    const size_t scratch = kOffDiag + pb + 256 + 256;
+    BATCH_CUDA(cudaMalloc(&d_scratch_, scratch), "cudaMalloc");
+    BATCH_CUDA(cudaMemsetAsync(d_scratch_, 0, scratch, stream_), "cudaMemset");
+    d_counters_ = static_cast<unsigned int *>(d_scratch_);
+    d_status_ = reinterpret_cast<int *>(static_cast<char *>(d_scratch_) + kOffStatus);
+    BATCH_CUDA(cudaMallocHost(reinterpret_cast<void **>(&h_result_), sizeof(DiagResult)), "cudaMallocHost");
+    device_bytes_ += scratch;
+    int maxg = launch::batch_max_grid(fast_, ty_);
+    if (maxg <= 0) {
+        err = "the batch kernel cannot be resident on this device";
+        return BUBBLE_ERR_CUDA;
+    }
+    if (o.max_grid > 0 && o.max_grid < maxg) maxg = o.max_grid;
+    max_grid_ = maxg;
+    return BUBBLE_OK;
+}
+
+int Batch::create(const bubble_spec *specs, uint32_t n, const bubble_batch_options *opt,
+                  std::unique_ptr<Batch> &out, std::string &err) {
+    if (n == 0) {
+        err = "a batch needs at least one lattice";
+        return BUBBLE_ERR_INVALID;
+    }
+    for (uint32_t k = 0; k < n; ++k) {
+        const std::string msg = check_spec(specs[k], specs[0].math);
+        if (!msg.empty()) {
+            err = "lattice " + std::to_string(k) + ": " + msg;
+            return BUBBLE_ERR_INVALID;
+        }
     }
     // admission: the whole batch against free memory (src/gpu/vram.rs:52-69)
     uint64_t need = 0;
@@ -168,54 +197,28 @@ int Batch::create(const bubble_spec *specs, uint32_t n, const bubble_batch_optio
         return BUBBLE_ERR_MEMORY;
     }
     std::unique_ptr<Batch> b(new Batch());
-    b->fast_ = fast;
-    b->ty_ = o.tile_y;
-    b->use_graph_ = o.use_graph != 0;
-    BATCH_CUDA(cudaStreamCreateWithFlags(&b->stream_, cudaStreamNonBlocking), "cudaStreamCreate");
-    b->lats_.resize(n);
+    int rc = b->setup(specs[0].math, opt, err);
+    if (rc != BUBBLE_OK) return rc;
     for (uint32_t k = 0; k < n; ++k) {
-        Lat &L = b->lats_[k];
-        L.spec = specs[k];
-        std::memcpy(L.grid, specs[k].grid, sizeof(L.grid));
-        L.cells = (uint64_t)L.grid[0] * L.grid[1] * L.grid[2];
-        L.P = params_of(L.spec.model, L.grid);
-        const Derived d = derive(L.spec.model);
-        L.dt = d.dt;
-        L.schedule = make_schedule(L.spec.nucleation, L.spec.bubbles, d.seed_radius, L.grid,
-                                   L.spec.nucleation_duration, L.spec.seed);
-        L.lz = default_chunk(L.grid, b->ty_);
-        const int rc = b->allocate(L, err);
+        uint32_t idx = 0;
+        rc = b->add(specs[k], &idx, err);
         if (rc != BUBBLE_OK) return rc;
     }
-    // work items, largest lattices first
-    b->item_order_.resize(n);
-    std::iota(b->item_order_.begin(), b->item_order_.end(), 0u);
-    std::stable_sort(b->item_order_.begin(), b->item_order_.end(),
-                     [&](uint32_t a, uint32_t c) { return b->lats_[a].cells > b->lats_[c].cells; });
-    const size_t lat_bytes = sizeof(BatchLattice) * n;
-    BATCH_CUDA(cudaMalloc(reinterpret_cast<void **>(&b->d_lat_), lat_bytes), "cudaMalloc");
-    BATCH_CUDA(cudaMallocHost(reinterpret_cast<void **>(&b->h_lat_), lat_bytes), "cudaMallocHost");
-    const size_t pb = (launch::diag_partials_bytes() + 255) & ~(size_t)255;
-    const size_t scratch = 256 + pb + 256 + 256;
-    BATCH_CUDA(cudaMalloc(&b->d_scratch_, scratch), "cudaMalloc");
-    BATCH_CUDA(cudaMemsetAsync(b->d_scratch_, 0, scratch, b->stream_), "cudaMemset");
-    b->d_counters_ = static_cast<unsigned int *>(b->d_scratch_);
-    b->d_status_ = reinterpret_cast<int *>(static_cast<char *>(b->d_scratch_) + 64);
-    BATCH_CUDA(cudaMallocHost(reinterpret_cast<void **>(&b->h_result_), sizeof(DiagResult)), "cudaMallocHost");
-    b->device_bytes_ += lat_bytes + scratch;
-    int maxg = launch::batch_max_grid(fast, b->ty_);
-    if (maxg <= 0) {
-        err = "the batch kernel cannot be resident on this device";
-        return BUBBLE_ERR_CUDA;
-    }
-    if (o.max_grid > 0 && o.max_grid < maxg) maxg = o.max_grid;
-    b->max_grid_ = maxg;
     b->plan_items();
-    if (o.autotune) {
-        const int rc = b->autotune(err);
+    if (!opt || opt->autotune) {
+        rc = b->autotune(err);
         if (rc != BUBBLE_OK) return rc;
     }
     BATCH_CUDA(cudaStreamSynchronize(b->stream_), "cudaStreamSynchronize");
+    out = std::move(b);
+    return BUBBLE_OK;
+}
+
+int Batch::create_empty(int math, const bubble_batch_options *opt, std::unique_ptr<Batch> &out,
+                        std::string &err) {
+    std::unique_ptr<Batch> b(new Batch());
+    const int rc = b->setup(math, opt, err);
+    if (rc != BUBBLE_OK) return rc;
     out = std::move(b);
     return BUBBLE_OK;
 }
@@ -233,6 +236,12 @@ Batch::~Batch() {
     if (stream_) cudaStreamDestroy(stream_);
 }
 
+uint32_t Batch::active_count() const {
+    uint32_t n = 0;
+    for (const auto &L : lats_) n += L.state != nullptr;
+    return n;
+}
+
 int Batch::allocate(Lat &L, std::string &err) {
     auto round_up = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t fb = round_up(L.cells * 8), ub = round_up(L.cells * 16);
@@ -244,7 +253,8 @@ int Batch::allocate(Lat &L, std::string &err) {
         err = std::string("device allocation of a batch lattice failed: ") + cudaGetErrorString(e);
         return BUBBLE_ERR_MEMORY;
     }
-    device_bytes_ += 3 * slot;
+    L.bytes = 3 * slot;
+    device_bytes_ += L.bytes;
     L.tma_ok = true;
     for (int k = 0; k < 3; ++k) {
         L.field[k] = static_cast<char *>(L.state) + k * slot;
@@ -258,14 +268,83 @@ int Batch::allocate(Lat &L, std::string &err) {
     return BUBBLE_OK;
 }
 
-// Items of a stage for the current z chunks, and the persistent grid.
+int Batch::add(const bubble_spec &spec, uint32_t *index, std::string &err) {
+    const std::string msg = check_spec(spec, math_);
+    if (!msg.empty()) {
+        err = msg;
+        return BUBBLE_ERR_INVALID;
+    }
+    Lat L;
+    L.spec = spec;
+    std::memcpy(L.grid, spec.grid, sizeof(L.grid));
+    L.cells = (uint64_t)L.grid[0] * L.grid[1] * L.grid[2];
+    L.P = params_of(spec.model, L.grid);
+    const Derived d = derive(spec.model);
+    L.dt = d.dt;
+    L.schedule = make_schedule(spec.nucleation, spec.bubbles, d.seed_radius, L.grid, spec.nucleation_duration,
+                               spec.seed);
+    L.lz = (int)std::min<uint32_t>(L.grid[2], (uint32_t)lz_cap_);
+    const int rc = allocate(L, err);
+    if (rc != BUBBLE_OK) return rc;
+    lats_.push_back(std::move(L));
+    *index = (uint32_t)(lats_.size() - 1);
+    dirty_ = true;
+    return BUBBLE_OK;
+}
+
+int Batch::remove(uint32_t k, std::string &err) {
+    if (!active(k)) {
+        err = "no active lattice at this index";
+        return BUBBLE_ERR_INVALID;
+    }
+    BATCH_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    Lat &L = lats_[k];
+    BATCH_CUDA(cudaFree(L.state), "cudaFree");
+    device_bytes_ -= L.bytes;
+    L.state = nullptr;
+    for (int s = 0; s < 3; ++s) L.field[s] = L.fluid[s] = nullptr;
+    L.schedule.clear();
+    L.schedule.shrink_to_fit();
+    dirty_ = true;
+    return BUBBLE_OK;
+}
+
+// Items of a stage for the active lattices (largest first) and the grid.
 void Batch::plan_items() {
+    item_order_.clear();
+    for (uint32_t k = 0; k < lats_.size(); ++k)
+        if (lats_[k].state) item_order_.push_back(k);
+    std::stable_sort(item_order_.begin(), item_order_.end(),
+                     [&](uint32_t a, uint32_t c) { return lats_[a].cells > lats_[c].cells; });
     n_items_ = 0;
-    for (const auto &L : lats_) {
+    for (uint32_t k : item_order_) {
+        const Lat &L = lats_[k];
         const int tiles = (int)((L.grid[0] + 31) / 32) * (int)((L.grid[1] + ty_ - 1) / ty_);
         n_items_ += tiles * (int)((L.grid[2] + L.lz - 1) / L.lz);
     }
-    grid_ = std::min(max_grid_, n_items_);
+    grid_ = std::max(1, std::min(max_grid_, n_items_));
+    dirty_ = false;
+}
+
+int Batch::ensure_capacity(size_t n, std::string &err) {
+    if (n <= capacity_) return BUBBLE_OK;
+    size_t cap = std::max<size_t>(n, capacity_ * 2);
+    cap = std::max<size_t>(cap, 16);
+    BATCH_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    if (exec_) cudaGraphExecDestroy(exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    exec_ = nullptr;
+    graph_ = nullptr;
+    graph_ok_ = false;  // the captured memcpy referenced the old buffers
+    if (d_lat_) cudaFree(d_lat_);
+    if (h_lat_) cudaFreeHost(h_lat_);
+    d_lat_ = nullptr;
+    h_lat_ = nullptr;
+    BATCH_CUDA(cudaMalloc(reinterpret_cast<void **>(&d_lat_), sizeof(BatchLattice) * cap), "cudaMalloc");
+    BATCH_CUDA(cudaMallocHost(reinterpret_cast<void **>(&h_lat_), sizeof(BatchLattice) * cap), "cudaMallocHost");
+    device_bytes_ += sizeof(BatchLattice) * (cap - capacity_);
+    capacity_ = cap;
+    return BUBBLE_OK;
 }
 
 // Chooses the z chunks of the batch by timing the batch itself.  The
@@ -352,6 +431,9 @@ uint64_t Batch::steps_until_event(const Lat &L, uint64_t cap) const {
 }
 
 int Batch::launch_chunk(uint64_t k, std::string &err) {
+    if (item_order_.empty() || k == 0) return BUBBLE_OK;
+    int rc = ensure_capacity(item_order_.size(), err);
+    if (rc != BUBBLE_OK) return rc;
     // the previous launch has consumed the pinned descriptors
     BATCH_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
     int begin = 0;
@@ -374,8 +456,8 @@ int Batch::launch_chunk(uint64_t k, std::string &err) {
         D.tma_ok = L.tma_ok ? 1 : 0;
         begin += D.tiles_xy * D.chunks;
     }
-    const size_t lat_bytes = sizeof(BatchLattice) * lats_.size();
-    const int n_lat = (int)lats_.size();
+    const size_t lat_bytes = sizeof(BatchLattice) * item_order_.size();
+    const int n_lat = (int)item_order_.size();
     auto enqueue = [&]() -> cudaError_t {
         cudaError_t e = cudaMemcpyAsync(d_lat_, h_lat_, lat_bytes, cudaMemcpyHostToDevice, stream_);
         if (e == cudaSuccess) e = cudaMemsetAsync(d_counters_, 0, 16, stream_);
@@ -385,7 +467,8 @@ int Batch::launch_chunk(uint64_t k, std::string &err) {
         return e;
     };
     if (use_graph_) {
-        if (!graph_ok_ || graph_steps_ != k) {
+        const auto key = std::make_tuple(k, n_lat, n_items_, grid_);
+        if (!graph_ok_ || graph_key_ != key) {
             if (exec_) cudaGraphExecDestroy(exec_);
             if (graph_) cudaGraphDestroy(graph_);
             exec_ = nullptr;
@@ -399,7 +482,7 @@ int Batch::launch_chunk(uint64_t k, std::string &err) {
                 graph_ = g;
                 if (cudaGraphInstantiate(&exec_, graph_, 0) == cudaSuccess) {
                     graph_ok_ = true;
-                    graph_steps_ = k;
+                    graph_key_ = key;
                 }
             } else if (g) {
                 cudaGraphDestroy(g);
@@ -421,17 +504,21 @@ int Batch::launch_chunk(uint64_t k, std::string &err) {
 }
 
 int Batch::advance(uint64_t steps, std::string &err) {
+    if (dirty_) plan_items();
     uint64_t done = 0;
     while (done < steps) {
         for (auto &L : lats_) {
+            if (!L.state) continue;
             const int rc = nucleate_due(L, err);
             if (rc != BUBBLE_OK) return rc;
         }
         uint64_t k = steps - done;
-        for (const auto &L : lats_) k = std::min(k, steps_until_event(L, k));
+        for (const auto &L : lats_)
+            if (L.state) k = std::min(k, steps_until_event(L, k));
         const int rc = launch_chunk(k, err);
         if (rc != BUBBLE_OK) return rc;
         for (auto &L : lats_) {
+            if (!L.state) continue;
             L.cur = (uint32_t)((L.cur + k) % 3);
             for (uint64_t j = 0; j < k; ++j) L.time += L.dt;
             L.steps += k;
@@ -454,13 +541,13 @@ int Batch::check_status(std::string &err) {
 }
 
 int Batch::diagnostics(uint32_t k, bubble_diag *out, std::string &err) {
-    if (k >= lats_.size()) {
-        err = "lattice index out of range";
+    if (!active(k)) {
+        err = "no active lattice at this index";
         return BUBBLE_ERR_INVALID;
     }
     const Lat &L = lats_[k];
     const size_t pb = (launch::diag_partials_bytes() + 255) & ~(size_t)255;
-    char *base = static_cast<char *>(d_scratch_) + 256;
+    char *base = static_cast<char *>(d_scratch_) + kOffDiag;
     unsigned int *ticket = reinterpret_cast<unsigned int *>(base + pb);
     DiagResult *res = reinterpret_cast<DiagResult *>(base + pb + 256);
     BATCH_CUDA(launch::diag_f32((const V2<float> *)L.field[L.cur], (const V4<float> *)L.fluid[L.cur], L.P, false,
@@ -495,8 +582,8 @@ int Batch::diagnostics(uint32_t k, bubble_diag *out, std::string &err) {
 }
 
 int Batch::copy_state(uint32_t k, float *field, float *fluid, std::string &err) {
-    if (k >= lats_.size()) {
-        err = "lattice index out of range";
+    if (!active(k)) {
+        err = "no active lattice at this index";
         return BUBBLE_ERR_INVALID;
     }
     const Lat &L = lats_[k];
@@ -507,8 +594,8 @@ int Batch::copy_state(uint32_t k, float *field, float *fluid, std::string &err) 
 }
 
 int Batch::load_state(uint32_t k, const float *field, const float *fluid, std::string &err) {
-    if (k >= lats_.size()) {
-        err = "lattice index out of range";
+    if (!active(k)) {
+        err = "no active lattice at this index";
         return BUBBLE_ERR_INVALID;
     }
     const Lat &L = lats_[k];
@@ -520,13 +607,14 @@ int Batch::load_state(uint32_t k, const float *field, const float *fluid, std::s
 
 void Batch::info(bubble_batch_info *out) const {
     std::memset(out, 0, sizeof(*out));
-    out->lattices = (uint32_t)lats_.size();
+    out->lattices = active_count();
     out->grid = (uint32_t)grid_;
     out->items = (uint32_t)n_items_;
     out->tile_y = ty_;
     out->graph = graph_ok_ ? 1 : 0;
     out->autotuned = autotuned_ ? 1 : 0;
-    for (const auto &L : lats_) out->cells += L.cells;
+    for (const auto &L : lats_)
+        if (L.state) out->cells += L.cells;
     out->launches = launches_;
     out->device_bytes = device_bytes_;
 }
