@@ -62,6 +62,18 @@ BUBBLE_DEV float rsqrt_approx(float x) {
     return r;
 }
 
+// Paired FP32 arithmetic of sm_100+ (two IEEE operations per instruction),
+// used by the FAST mode on the (x, y) and (z, w) halves of 4-vectors.
+BUBBLE_DEV float2 lo2(const V4<float> &v) { return make_float2(v.x, v.y); }
+BUBBLE_DEV float2 hi2(const V4<float> &v) { return make_float2(v.z, v.w); }
+BUBBLE_DEV V4<float> v4of(float2 a, float2 b) { return V4<float>{a.x, a.y, b.x, b.y}; }
+BUBBLE_DEV float2 bc2(float s) { return make_float2(s, s); }
+BUBBLE_DEV float2 p_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+// a - b as a + b * (-1): exact product, one rounding
+BUBBLE_DEV float2 p_sub(float2 a, float2 b) { return __ffma2_rn(b, bc2(-1.0f), a); }
+BUBBLE_DEV float2 p_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+BUBBLE_DEV float2 p_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
 // ---------------------------------------------------------------------------
 //  Potential (shaders/potential.wgsl:38-47)
 // ---------------------------------------------------------------------------
@@ -207,6 +219,35 @@ BUBBLE_DEV V4<R> half_step(const V4<R> &q, const V4<R> &s, R sign) {
                  q.z + sign * (R(0.5) * s.z), q.w + sign * (R(0.5) * s.w)};
 }
 
+// The two sanitised face states of a cell along one axis from its
+// neighbours qm, qp: lo = q - s/2 (face i-1/2), hi = q + s/2 (face i+1/2),
+// s the MC-limited slope (shaders/step.wgsl:125-144).
+template <typename R, bool FAST>
+BUBBLE_DEV void face_states(const V4<R> &qm, const V4<R> &q, const V4<R> &qp, R p_floor, R vmax2, V4<R> &lo,
+                            V4<R> &hi) {
+    if constexpr (FAST && sizeof(R) == 4) {
+        const float2 qa = lo2(q), qb = hi2(q);
+        const float2 dma = p_sub(qa, lo2(qm)), dmb = p_sub(qb, hi2(qm));
+        const float2 dpa = p_sub(lo2(qp), qa), dpb = p_sub(hi2(qp), qb);
+        const float2 ha = p_mul(p_add(dma, dpa), bc2(0.5f)), hb = p_mul(p_add(dmb, dpb), bc2(0.5f));
+        const float2 pa = p_mul(dma, dpa), pb = p_mul(dmb, dpb);
+        const float2 ma = p_mul(make_float2(fminf(fabsf(dma.x), fabsf(dpa.x)), fminf(fabsf(dma.y), fabsf(dpa.y))),
+                                bc2(2.0f));
+        const float2 mb = p_mul(make_float2(fminf(fabsf(dmb.x), fabsf(dpb.x)), fminf(fabsf(dmb.y), fabsf(dpb.y))),
+                                bc2(2.0f));
+        const float2 sa = make_float2(pa.x > 0.0f ? copysignf(fminf(fabsf(ha.x), ma.x), dma.x) : 0.0f,
+                                      pa.y > 0.0f ? copysignf(fminf(fabsf(ha.y), ma.y), dma.y) : 0.0f);
+        const float2 sb = make_float2(pb.x > 0.0f ? copysignf(fminf(fabsf(hb.x), mb.x), dmb.x) : 0.0f,
+                                      pb.y > 0.0f ? copysignf(fminf(fabsf(hb.y), mb.y), dmb.y) : 0.0f);
+        lo = sanitise(v4of(p_fma(sa, bc2(-0.5f), qa), p_fma(sb, bc2(-0.5f), qb)), p_floor, vmax2);
+        hi = sanitise(v4of(p_fma(sa, bc2(0.5f), qa), p_fma(sb, bc2(0.5f), qb)), p_floor, vmax2);
+    } else {
+        const V4<R> s = limit_slope4<R, FAST>(v4_sub(q, qm), v4_sub(qp, q));
+        lo = sanitise(half_step(q, s, R(-1)), p_floor, vmax2);
+        hi = sanitise(half_step(q, s, R(1)), p_floor, vmax2);
+    }
+}
+
 // ---------------------------------------------------------------------------
 //  HLL face flux (shaders/step.wgsl:74-90 with eos.wgsl:129-176)
 // ---------------------------------------------------------------------------
@@ -237,7 +278,10 @@ BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2) {
         // E + p = w W^2, so the energy flux is w vd.
         const R om = R(1.0) - v2;
         const R w = (R(4.0) * p) * rcp_approx(om);
-        s.u = V4<R>{w - p, w * vx, w * vy, w * vz};
+        {
+            const float2 uzw = p_mul(bc2(w), make_float2(vy, vz));
+            s.u = V4<R>{w - p, w * vx, uzw.x, uzw.y};
+        }
         const R inv_den = rcp_approx(R(1.0) - v2 * cs2);
         const R tt = R(1.0) - (R(2.0) / R(3.0)) * (vd * vd) - cs2 * v2;
         const R rad = vmax(om * tt, R(0.0));
@@ -246,7 +290,7 @@ BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2) {
         const R b = cs * sqrt_approx(rad) * inv_den;
         s.lm = a - b;
         s.lp = a + b;
-        s.f = V4<R>{w * vd, s.u.y * vd, s.u.z * vd, s.u.w * vd};
+        s.f = v4of(p_mul(make_float2(w, s.u.y), bc2(vd)), p_mul(hi2(s.u), bc2(vd)));
         if constexpr (AXIS == 0) s.f.y = s.f.y + p;
         if constexpr (AXIS == 1) s.f.z = s.f.z + p;
         if constexpr (AXIS == 2) s.f.w = s.f.w + p;
@@ -281,10 +325,11 @@ BUBBLE_DEV V4<R> hll_flux(const V4<R> &ql, const V4<R> &qr, R zmax2) {
     const R smm = s_min * s_max;
     if constexpr (FAST) {
         const R inv = rcp_approx(den);
-        return V4<R>{(s_max * L.f.x - s_min * Rt.f.x + smm * (Rt.u.x - L.u.x)) * inv,
-                     (s_max * L.f.y - s_min * Rt.f.y + smm * (Rt.u.y - L.u.y)) * inv,
-                     (s_max * L.f.z - s_min * Rt.f.z + smm * (Rt.u.z - L.u.z)) * inv,
-                     (s_max * L.f.w - s_min * Rt.f.w + smm * (Rt.u.w - L.u.w)) * inv};
+        float2 a = p_mul(bc2(smm), p_sub(lo2(Rt.u), lo2(L.u)));
+        float2 b = p_mul(bc2(smm), p_sub(hi2(Rt.u), hi2(L.u)));
+        a = p_fma(bc2(-s_min), lo2(Rt.f), p_fma(bc2(s_max), lo2(L.f), a));
+        b = p_fma(bc2(-s_min), hi2(Rt.f), p_fma(bc2(s_max), hi2(L.f), b));
+        return v4of(p_mul(a, bc2(inv)), p_mul(b, bc2(inv)));
     } else {
         return V4<R>{(s_max * L.f.x - s_min * Rt.f.x + smm * (Rt.u.x - L.u.x)) / den,
                      (s_max * L.f.y - s_min * Rt.f.y + smm * (Rt.u.y - L.u.y)) / den,

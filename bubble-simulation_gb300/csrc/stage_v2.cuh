@@ -258,10 +258,7 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
     auto z_states = [&](int p, int n, V4<R> &lo, V4<R> &hi) {
         const int i = n % TX, j = n / TX;
         const int c = (j + 2) * PW + (i + 2);
-        const V4<R> q = prim_slot(p)[c];
-        const V4<R> s = limit_slope4<R, FAST>(v4_sub(q, prim_slot(p - 1)[c]), v4_sub(prim_slot(p + 1)[c], q));
-        lo = sanitise(half_step(q, s, R(-1)), P.p_floor, zmax2);
-        hi = sanitise(half_step(q, s, R(1)), P.p_floor, zmax2);
+        face_states<R, FAST>(prim_slot(p - 1)[c], prim_slot(p)[c], prim_slot(p + 1)[c], P.p_floor, zmax2, lo, hi);
     };
 
     // ---- prologue ----------------------------------------------------------
@@ -374,20 +371,20 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
                     const int i = q - jj * TX;
                     const int c = (jj + 1) * PW + (i + 2);
                     const V4<R> *pr = prim_slot(z);
-                    const V4<R> qc = pr[c];
-                    const V4<R> s = limit_slope4<R, FAST>(v4_sub(qc, pr[c - PW]), v4_sub(pr[c + PW], qc));
-                    ylo[jj * TX + i] = sanitise(half_step(qc, s, R(-1)), P.p_floor, zmax2);
-                    yhi[jj * TX + i] = sanitise(half_step(qc, s, R(1)), P.p_floor, zmax2);
+                    V4<R> lo, hi;
+                    face_states<R, FAST>(pr[c - PW], pr[c], pr[c + PW], P.p_floor, zmax2, lo, hi);
+                    ylo[jj * TX + i] = lo;
+                    yhi[jj * TX + i] = hi;
                 } else {
                     const int q = kk - L::X_Z - L::X_Y;
                     const int j = q / (TX + 2);
                     const int ii = q - j * (TX + 2);  // cell column ii-1
                     const int c = (j + 2) * PW + (ii + 1);
                     const V4<R> *pr = prim_slot(z);
-                    const V4<R> qc = pr[c];
-                    const V4<R> s = limit_slope4<R, FAST>(v4_sub(qc, pr[c - 1]), v4_sub(pr[c + 1], qc));
-                    xlo[j * (TX + 2) + ii] = sanitise(half_step(qc, s, R(-1)), P.p_floor, zmax2);
-                    xhi[j * (TX + 2) + ii] = sanitise(half_step(qc, s, R(1)), P.p_floor, zmax2);
+                    V4<R> lo, hi;
+                    face_states<R, FAST>(pr[c - 1], pr[c], pr[c + 1], P.p_floor, zmax2, lo, hi);
+                    xlo[j * (TX + 2) + ii] = lo;
+                    xhi[j * (TX + 2) + ii] = hi;
                 }
             }
         }
