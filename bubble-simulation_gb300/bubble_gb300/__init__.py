@@ -18,7 +18,8 @@ from ._lib import BubbleError, check, load
 
 __all__ = ["Model", "SimulationSpec", "Simulation", "Diagnostics", "make_schedule", "derived",
            "validate_model", "stage_slots", "rk3_coefficients", "lattice_bytes", "max_cubic_size",
-           "vram_query", "vram_available", "lattice_budget", "BubbleError", "load"]
+           "vram_query", "vram_available", "lattice_budget", "BubbleError", "load", "render_settings", "camera",
+           "render_view", "write_png"]
 
 
 @dataclass
@@ -280,6 +281,70 @@ class Simulation:
         fluid = np.ascontiguousarray(fluid, dtype=self._dtype).reshape(n, 4)
         fn = self._L.bubble_load_state_f64 if self._dtype == np.float64 else self._L.bubble_load_state
         check(fn(self._h, field.ctypes.data, fluid.ctypes.data))
+
+    # -- visualisation (include/bubble_render.h) ------------------------------
+    def visualise(self):
+        """record_visualisation (src/gpu/sim.rs:918-942) into the vis texture."""
+        check(self._L.bubble_visualise(self._h))
+
+    def vis_texture(self) -> np.ndarray:
+        """The vis texture as (nz, ny, nx, 4) uint16 binary16 bits."""
+        nx, ny, nz = self.grid
+        out = np.empty((nz, ny, nx, 4), dtype=np.uint16)
+        check(self._L.bubble_vis_copy(self._h, out.ctypes.data))
+        return out
+
+    def render(self, settings: "_lib.RenderSettings | None" = None, camera: "_lib.Camera | None" = None,
+               size: tuple = (1280, 960), frame: int = 1) -> np.ndarray:
+        """One frame of the volume renderer: (height, width, 4) uint8."""
+        settings = settings or render_settings()
+        w, h = size
+        out = np.empty((h, w, 4), dtype=np.uint8)
+        check(self._L.bubble_render(self._h, ctypes.byref(settings), ctypes.byref(camera) if camera else None,
+                                    w, h, frame, out.ctypes.data))
+        return out
+
+    def render_png(self, path: str, settings: "_lib.RenderSettings | None" = None, size: tuple = (1280, 960)):
+        """capture::render_to_png (src/capture.rs:19-117)."""
+        settings = settings or render_settings()
+        check(self._L.bubble_render_png(self._h, ctypes.byref(settings), size[0], size[1], str(path).encode()))
+
+
+def render_settings(field: str | None = None) -> _lib.RenderSettings:
+    """RenderSettings::default, or RenderSettings::with_field(field)."""
+    L = load()
+    s = _lib.RenderSettings()
+    if field is None:
+        check(L.bubble_render_settings_default(ctypes.byref(s)))
+    else:
+        check(L.bubble_render_settings_with_field(_lib.FIELDS[field], ctypes.byref(s)))
+    return s
+
+
+def camera(half_extent: Sequence[float] | None = None) -> _lib.Camera:
+    """OrbitCamera::default, framed on a box of `half_extent` if given."""
+    L = load()
+    c = _lib.Camera()
+    check(L.bubble_camera_default(ctypes.byref(c)))
+    if half_extent is not None:
+        check(L.bubble_camera_frame_box(ctypes.byref(c), (ctypes.c_float * 3)(*half_extent)))
+    return c
+
+
+def render_view(grid: Sequence[int], settings: _lib.RenderSettings, size: tuple, frame: int = 1,
+                cam: _lib.Camera | None = None) -> np.ndarray:
+    """The 176-byte view uniform of one frame as 44 float32."""
+    v = _lib.View()
+    check(load().bubble_render_view((ctypes.c_uint32 * 3)(*grid), ctypes.byref(settings),
+                                    ctypes.byref(cam) if cam else None, size[0], size[1], frame, ctypes.byref(v)))
+    return np.frombuffer(bytes(v), dtype=np.float32).copy()
+
+
+def write_png(path: str, rgba: np.ndarray):
+    rgba = np.ascontiguousarray(rgba, dtype=np.uint8)
+    h, w, c = rgba.shape
+    assert c == 4
+    check(load().bubble_write_png(str(path).encode(), rgba.ctypes.data, w, h))
 
 
 class Batch:

@@ -1,4 +1,4 @@
-"""ctypes declarations of include/bubble.h and include/bubble_ext.h.
+"""ctypes declarations of include/bubble*.h.
 
 Loads lib/libbubble_gb300.so from this package's source tree.  There is no
 fallback: if the library has not been built, loading raises with the build
@@ -107,11 +107,36 @@ class VramInfo(ctypes.Structure):
                 ("used", ctypes.c_uint64), ("has_budget", ctypes.c_int32)]
 
 
+FIELDS = {"phi": 0, "speed": 1, "temperature": 2, "kinetic": 3}
+COLORMAPS = {"viridis": 0, "inferno": 1, "signed": 2}
+
+
+class RenderSettings(ctypes.Structure):
+    _fields_ = [("field_mode", ctypes.c_int32), ("colormap", ctypes.c_int32), ("iso_level", ctypes.c_float),
+                ("wall_opacity", ctypes.c_float), ("samples_per_cell", ctypes.c_float), ("exposure", ctypes.c_float),
+                ("field_gain", ctypes.c_float), ("absorption", ctypes.c_float), ("show_iso", ctypes.c_int32),
+                ("show_volume", ctypes.c_int32), ("show_box", ctypes.c_int32), ("background", ctypes.c_float),
+                ("clip_axis", ctypes.c_int32), ("clip_pos", ctypes.c_float)]
+
+
+class Camera(ctypes.Structure):
+    _fields_ = [("target", ctypes.c_float * 3), ("distance", ctypes.c_float), ("yaw", ctypes.c_float),
+                ("pitch", ctypes.c_float), ("fov_y", ctypes.c_float), ("znear", ctypes.c_float),
+                ("zfar", ctypes.c_float)]
+
+
+class View(ctypes.Structure):
+    _fields_ = [("inv_view_proj", ctypes.c_float * 16)] + \
+               [(n, ctypes.c_float * 4) for n in ("cam_pos", "box_half", "grid", "render0", "render1", "render2",
+                                                  "render3")]
+
+
 # (name, restype, argtypes) of every exported symbol declared in include/*.h
 _P = ctypes.c_void_p
 _U32P = ctypes.POINTER(ctypes.c_uint32)
 _U64P = ctypes.POINTER(ctypes.c_uint64)
 _I32P = ctypes.POINTER(ctypes.c_int32)
+_F32P = ctypes.POINTER(ctypes.c_float)
 SIGNATURES = [
     ("bubble_model_default", None, [ctypes.POINTER(Model)]),
     ("bubble_model_validate", ctypes.c_int, [ctypes.POINTER(Model)]),
@@ -184,6 +209,28 @@ SIGNATURES = [
     ("bubble_server_poll", ctypes.c_int, [_P, ctypes.POINTER(ServerResult), ctypes.c_uint64, _U64P]),
     ("bubble_server_stats_get", ctypes.c_int, [_P, ctypes.POINTER(ServerStats)]),
     ("bubble_server_now", ctypes.c_double, [_P]),
+    # bubble_render.h
+    ("bubble_render_settings_default", ctypes.c_int, [ctypes.POINTER(RenderSettings)]),
+    ("bubble_render_settings_with_field", ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(RenderSettings)]),
+    ("bubble_camera_default", ctypes.c_int, [ctypes.POINTER(Camera)]),
+    ("bubble_camera_frame_box", ctypes.c_int, [ctypes.POINTER(Camera), _F32P]),
+    ("bubble_camera_orbit", ctypes.c_int, [ctypes.POINTER(Camera), ctypes.c_float, ctypes.c_float]),
+    ("bubble_camera_pan", ctypes.c_int, [ctypes.POINTER(Camera), ctypes.c_float, ctypes.c_float]),
+    ("bubble_camera_zoom", ctypes.c_int, [ctypes.POINTER(Camera), ctypes.c_float]),
+    ("bubble_camera_dolly", ctypes.c_int, [ctypes.POINTER(Camera), ctypes.c_float]),
+    ("bubble_camera_eye", ctypes.c_int, [ctypes.POINTER(Camera), _F32P]),
+    ("bubble_camera_basis", ctypes.c_int, [ctypes.POINTER(Camera), _F32P, _F32P, _F32P]),
+    ("bubble_camera_view_proj", ctypes.c_int, [ctypes.POINTER(Camera), ctypes.c_float, _F32P]),
+    ("bubble_render_box", ctypes.c_int, [_U32P, _F32P, _F32P]),
+    ("bubble_render_view", ctypes.c_int, [_U32P, ctypes.POINTER(RenderSettings), ctypes.POINTER(Camera),
+                                          ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(View)]),
+    ("bubble_visualise", ctypes.c_int, [_P]),
+    ("bubble_vis_copy", ctypes.c_int, [_P, _P]),
+    ("bubble_render", ctypes.c_int, [_P, ctypes.POINTER(RenderSettings), ctypes.POINTER(Camera), ctypes.c_uint32,
+                                     ctypes.c_uint32, ctypes.c_uint32, _P]),
+    ("bubble_render_png", ctypes.c_int, [_P, ctypes.POINTER(RenderSettings), ctypes.c_uint32, ctypes.c_uint32,
+                                         ctypes.c_char_p]),
+    ("bubble_write_png", ctypes.c_int, [ctypes.c_char_p, _P, ctypes.c_uint32, ctypes.c_uint32]),
 ]
 
 _lib = None

@@ -53,8 +53,10 @@ KERNEL_UNITS = {
     "kernels_fast.cu": ["--fmad=true"],
     "kernels_f64.cu": ["--fmad=false"],
     "diag_noalloc.cu": ["--fmad=false"],
+    "render.cu": ["--fmad=false"],
 }
-HOST_UNITS = ["physics.cpp", "simulation.cpp", "capi.cpp", "tma.cpp", "batch.cpp", "capi_batch.cpp", "server.cpp"]
+HOST_UNITS = ["physics.cpp", "simulation.cpp", "capi.cpp", "tma.cpp", "batch.cpp", "capi_batch.cpp", "server.cpp",
+              "render_host.cpp"]
 CLI_UNITS = ["headless.cpp"]
 HEADERS = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
 

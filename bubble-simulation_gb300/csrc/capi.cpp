@@ -11,11 +11,7 @@
 #include "../../include/bubble.h"
 #include "../../include/bubble_ext.h"
 #include "physics.h"
-#include "simulation.h"
-
-struct bubble_sim {
-    std::unique_ptr<bubble::Simulation> impl;
-};
+#include "sim_handle.h"
 
 namespace {
 thread_local std::string g_last_error;

@@ -3,9 +3,11 @@
 // Mirrors the reference's command line (src/config.rs:193-297, validation
 // src/config.rs:333-360, dispatch src/main.rs:27-34) and its headless run
 // (src/headless.rs:23-150): the same banner, table, drift baseline (first
-// report after every bubble is in), R_eq and throughput line.  The
-// interactive window and --screenshot need a renderer and are not part of
-// this build; they are rejected with an error.
+// report after every bubble is in), R_eq and throughput line.
+// --screenshot renders one frame with the CUDA volume renderer and writes
+// it as a PNG (src/capture.rs:19-117, called from src/headless.rs:102-114).
+// The interactive window is not part of this build and is rejected with an
+// error.
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -15,6 +17,7 @@
 #include <vector>
 
 #include "../../include/bubble.h"
+#include "../../include/bubble_render.h"
 
 namespace {
 
@@ -34,6 +37,8 @@ struct Args {
     bool has_report_every = false;
     unsigned long long report_every = 0;
     std::string screenshot;
+    uint32_t screenshot_size[2] = {1280, 960};
+    int field = BUBBLE_FIELD_KINETIC;
     int precision = BUBBLE_PRECISION_SINGLE;
     int math = BUBBLE_MATH_FAST;
 };
@@ -104,8 +109,13 @@ void usage() {
         "  --report-every K          report interval [default: max(N/20, 1)]\n"
         "  --precision MODE          single|mixed|double [default: single]\n"
         "  --math MODE               fast|strict [default: fast]\n"
-        "  --field F, --no-vsync     accepted for compatibility; no effect headless\n");
+        "  --field F                 phi|speed|temperature|kinetic, for --screenshot [default: kinetic]\n"
+        "  --screenshot PATH         render one frame to this PNG and exit\n"
+        "  --screenshot-size WxH     resolution of --screenshot [default: 1280x960]\n"
+        "  --no-vsync                accepted for compatibility; no effect headless\n");
 }
+
+bool parse_size(const std::string &s, uint32_t out[2], std::string &msg);
 
 Args parse(int argc, char **argv) {
     Args a;
@@ -158,7 +168,19 @@ Args parse(int argc, char **argv) {
             a.has_report_every = true;
             a.report_every = parse_u(next(), "--report-every");
         } else if (f == "--screenshot") a.screenshot = next();
-        else if (f == "--screenshot-size" || f == "--field") (void)next();
+        else if (f == "--screenshot-size") {
+            const std::string v = next();
+            std::string msg;
+            if (!parse_size(v, a.screenshot_size, msg))
+                die("invalid value '" + v + "' for '--screenshot-size <SCREENSHOT_SIZE>': " + msg);
+        } else if (f == "--field") {
+            const std::string m = next();
+            if (m == "phi") a.field = BUBBLE_FIELD_PHI;
+            else if (m == "speed") a.field = BUBBLE_FIELD_SPEED;
+            else if (m == "temperature") a.field = BUBBLE_FIELD_TEMPERATURE;
+            else if (m == "kinetic") a.field = BUBBLE_FIELD_KINETIC;
+            else die("invalid value '" + m + "' for '--field'");
+        }
         else if (f == "--no-vsync") {
         } else if (f == "--precision") {
             const std::string m = next();
@@ -176,6 +198,34 @@ Args parse(int argc, char **argv) {
         }
     }
     return a;
+}
+
+// parse_size (src/config.rs:181-192): WIDTHxHEIGHT (or X), both positive.
+bool parse_size(const std::string &s, uint32_t out[2], std::string &msg) {
+    const size_t c = s.find_first_of("xX");
+    if (c == std::string::npos) {
+        msg = "`" + s + "` is not a size; expected WIDTHxHEIGHT";
+        return false;
+    }
+    const std::string parts[2] = {s.substr(0, c), s.substr(c + 1)};
+    const char *what[2] = {"width", "height"};
+    for (int k = 0; k < 2; ++k) {
+        std::string p = parts[k];
+        const size_t a = p.find_first_not_of(" \t"), b = p.find_last_not_of(" \t");
+        p = a == std::string::npos ? std::string() : p.substr(a, b - a + 1);
+        char *end = nullptr;
+        const unsigned long long v = p.empty() ? 0 : std::strtoull(p.c_str(), &end, 10);
+        if (p.empty() || *end != '\0' || p[0] == '-' || p[0] == '+' || v > 0xffffffffULL) {
+            msg = std::string(what[k]) + ": invalid digit found in string";
+            return false;
+        }
+        if (v == 0) {
+            msg = std::string(what[k]) + " must be positive";
+            return false;
+        }
+        out[k] = (uint32_t)v;
+    }
+    return true;
 }
 
 bubble_model model_of(const Args &a) {
@@ -316,6 +366,18 @@ int run(const Args &a, unsigned long long steps, unsigned long long every) {
         std::printf("\n%llu steps in %.2f s  (%.1f steps/s, %.2f G cell-updates/s)\n", steps, elapsed,
                     (double)steps / elapsed, cell_steps / elapsed / 1e9);
     }
+    if (!a.screenshot.empty()) {
+        // render_to_png (src/capture.rs:19-117) of the current state
+        bubble_render_settings rs;
+        bubble_render_settings_with_field(a.field, &rs);
+        if (bubble_render_png(sim, &rs, a.screenshot_size[0], a.screenshot_size[1], a.screenshot.c_str()) !=
+            BUBBLE_OK) {
+            const std::string msg = bubble_last_error();
+            bubble_destroy(sim);
+            die(msg, 1);
+        }
+        std::printf("wrote %s (%ux%u)\n", a.screenshot.c_str(), a.screenshot_size[0], a.screenshot_size[1]);
+    }
     bubble_destroy(sim);
     return 0;
 }
@@ -325,11 +387,10 @@ int run(const Args &a, unsigned long long steps, unsigned long long every) {
 int main(int argc, char **argv) {
     const Args a = parse(argc, argv);
     validate(a);
-    if (!a.screenshot.empty())
-        die("--screenshot needs the volume renderer, which this build does not include", 2);
-    if (!a.has_headless)
+    // src/main.rs:30-34: --headless or --screenshot run windowless
+    if (!a.has_headless && a.screenshot.empty())
         die("the interactive window is not part of this build; run with --headless N", 2);
-    const unsigned long long steps = a.headless;
+    const unsigned long long steps = a.has_headless ? a.headless : 0;
     unsigned long long every = a.has_report_every ? a.report_every : steps / 20;
     if (every < 1) every = 1;
     return run(a, steps, every);

@@ -121,6 +121,7 @@ Simulation::~Simulation() {
 }
 
 void Simulation::release() {
+    release_vis();
     if (state_) cudaFree(state_);
     if (prim_) cudaFree(prim_);
     if (scratch_) cudaFree(scratch_);
@@ -286,8 +287,9 @@ int Simulation::resize(const uint32_t grid[3], std::string &err) {
 
 int Simulation::set_tile(TileShape t, std::string &err) {
     const bool strict = !is_f64() && spec_.math == BUBBLE_MATH_STRICT;
-    if (t.tx != 32 || !launch::fused_shape_supported(is_f64(), t.ty) || !launch::v2_shape_supported(is_f64(), t.ty) ||
-        (strict && t.ty != 8) || t.lz < 1) {
+    // the synchronous-staging and strict kernels are built for fewer shapes
+    // than the default one; their launches check the shape themselves
+    if (t.tx != 32 || !launch::v2_shape_supported(is_f64(), t.ty) || (strict && t.ty != 8) || t.lz < 1) {
         err = "unsupported tile shape";
         return BUBBLE_ERR_INVALID;
     }

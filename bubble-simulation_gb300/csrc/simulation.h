@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/bubble.h"
+#include "../../include/bubble_render.h"
 #include "params.h"
 #include "physics.h"
 #include "tma.h"
@@ -73,6 +74,22 @@ class Simulation {
     // Kernel launches issued since creation (init, nucleate, stage, diag).
     uint64_t launches() const { return launches_; }
 
+    // Checkpoint and resume (checkpoint.cpp): the current slot's state, the
+    // schedule and the clock, written to a file; `restore` reloads one into
+    // this simulation (resizing it if the grid differs).
+    int save_checkpoint(const std::string &path, std::string &err);
+    int restore_checkpoint(const std::string &path, std::string &err);
+    // Reads the spec stored in a checkpoint file without creating anything.
+    static int checkpoint_spec(const std::string &path, bubble_spec &spec, std::string &err);
+
+    // Visualisation (render_host.cpp): record_visualisation
+    // (src/gpu/sim.rs:918-942) into a half4 CUDA array allocated on first
+    // use, its readback, and one frame of the volume renderer.
+    int visualise(std::string &err);
+    int vis_copy(uint16_t *host_rgba16, std::string &err);
+    int render(const bubble_view &view, uint32_t width, uint32_t height, uint8_t *host_rgba8,
+               std::string &err);
+
    private:
     Simulation() = default;
     int allocate(std::string &err);
@@ -114,6 +131,15 @@ class Simulation {
     StageMaps maps_[3];         // TMA maps of each slot as a stage input
     bool tma_ok_ = false;
     int check_status(std::string &err);
+
+    // visualisation texture (render_host.cpp); released with the lattice
+    void release_vis();
+    cudaArray_t vis_array_ = nullptr;
+    cudaSurfaceObject_t vis_surf_ = 0;
+    cudaTextureObject_t vis_tex_ = 0;
+    uint64_t vis_bytes_ = 0;
+    void *image_ = nullptr;  // device RGBA8 frame
+    size_t image_bytes_ = 0;
 
     cudaStream_t stream_ = nullptr;
     bool own_stream_ = false;

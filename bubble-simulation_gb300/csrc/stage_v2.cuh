@@ -105,8 +105,11 @@ template <typename R, int TY>
 struct V2Layout {
     static constexpr int TX = 32;
     static constexpr int PW = TX + 4, PH = TY + 4, PC = PW * PH, NC = TX * TY;
-    static constexpr int NT = TY == 8 ? 320 : 192;
-    static constexpr int MIN_BLOCKS = sizeof(R) == 4 ? 2 : 1;
+    // TY = 16 (640 threads, one CTA per SM) was measured no faster than TY = 8
+    // at 512^3 (17.09 vs 17.01 ms per step): the smaller halo share is lost to
+    // barrier waits with no second CTA to issue from.
+    static constexpr int NT = TY == 16 ? 640 : (TY == 8 ? 320 : 192);
+    static constexpr int MIN_BLOCKS = (sizeof(R) == 4 && TY <= 8) ? 2 : 1;
     // phase X: combine of the previous plane, then face states
     static constexpr int X_C = NC, X_Z = NC, X_Y = TX * (TY + 2), X_X = (TX + 2) * TY;
     static constexpr int X_TOTAL = X_C + X_Z + X_Y + X_X;

@@ -16,12 +16,17 @@
 //   init main                    shaders/init.wgsl:18-26
 //   nucleate main, min_image     shaders/nucleate.wgsl:51-85
 //   cell_contribution, reduce    shaders/reduce.wgsl:49-140 (sums in FP64)
+//   vis main                     shaders/vis.wgsl:30-55 (binary16 round to nearest even)
+//   fs_main and helpers          shaders/volume.wgsl:80-381, with the
+//                                sampler of src/gpu/render.rs:206-218
+//                                (trilinear, clamp to edge) in software
 // Built with -ffp-contract=off so every operation is one IEEE rounding.
 // WGSL's tanh has implementation-defined accuracy; the oracle uses the
 // Cody-Waite / Taylor tanh described at oracle_tanh (accurate to a few
 // units in 1e-16), which the CUDA library evaluates with the same
 // operations, so nucleated fields compare bit for bit.  Its FP64 relative
 // error is below 1e-15 (tests/test_oracle_pins.py).
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -489,6 +494,324 @@ void reduce_all(const SimParams<R> &P, const R *field, const R *fluid, const R *
     *max_v = vm;
 }
 
+
+// ---------------------------------------------------------------------------
+//  vis.wgsl and volume.wgsl (the headless screenshot path)
+// ---------------------------------------------------------------------------
+// IEEE binary32 -> binary16, round to nearest even (the rgba16float store).
+inline uint16_t f32_to_f16(float f) {
+    uint32_t x;
+    std::memcpy(&x, &f, 4);
+    const uint32_t sign = (x >> 16) & 0x8000u;
+    const uint32_t ax = x & 0x7fffffffu;
+    if (ax >= 0x7f800000u) return (uint16_t)(sign | 0x7c00u | (ax > 0x7f800000u ? 0x200u : 0u));
+    if (ax >= 0x477ff000u) return (uint16_t)(sign | 0x7c00u);  // >= 65520 rounds to infinity
+    if (ax < 0x38800000u) {                                    // below 2^-14: subnormal or zero
+        const float v = std::fabs(f) * 16777216.0f;            // exact: scaled by 2^24
+        return (uint16_t)(sign | (uint32_t)std::nearbyint(v));
+    }
+    const uint32_t mant = ax & 0x7fffffu;
+    const uint32_t e = (ax >> 23) - 127u + 15u;
+    uint32_t h = (e << 10) | (mant >> 13);
+    const uint32_t rem = mant & 0x1fffu;
+    if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) h += 1u;
+    return (uint16_t)(sign | h);
+}
+
+inline float f16_to_f32(uint16_t h) {
+    const uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
+    const uint32_t e = (h >> 10) & 0x1fu, m = h & 0x3ffu;
+    float v;
+    if (e == 0) v = std::ldexp((float)m, -24);
+    else if (e == 31) v = m ? NAN : INFINITY;
+    else v = std::ldexp((float)(m | 0x400u), (int)e - 25);
+    uint32_t b;
+    std::memcpy(&b, &v, 4);
+    b |= sign;
+    std::memcpy(&v, &b, 4);
+    return v;
+}
+
+// vis main (shaders/vis.wgsl:30-55) over a primitives buffer from
+// primitives_all; out = nx*ny*nz half4 texels.
+template <typename R>
+void vis_all(const SimParams<R> &P, const R *field, const R *fluid, const R *prim, uint16_t *out) {
+    const int64_t n = (int64_t)P.nx * P.ny * P.nz;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        const R phi = field[2 * i];
+        const R vx = prim[4 * i], vy = prim[4 * i + 1], vz = prim[4 * i + 2], p = prim[4 * i + 3];
+        const R e_lab = wmax(fluid[4 * i], P.e_floor);
+        const R vv = vx * vx + vy * vy + vz * vz;
+        const R speed = std::sqrt(vv);
+        const R x = R(3.0) * wmax(p, P.p_floor) / P.a_rad;  // eos_temperature (shaders/eos.wgsl:65-69)
+        const R temp = std::sqrt(std::sqrt(x));
+        const R kinetic = (e_lab + p) * vv;
+        out[4 * i + 0] = f32_to_f16((float)(phi / P.phi_b));
+        out[4 * i + 1] = f32_to_f16((float)speed);
+        out[4 * i + 2] = f32_to_f16((float)(temp / P.t_ref - R(1.0)));
+        out[4 * i + 3] = f32_to_f16((float)(kinetic / P.e_ref));
+    }
+}
+
+// The ViewUniform of shaders/volume.wgsl:22-31 as 44 floats.
+struct View {
+    float m[16];
+    float cam[4], box[4], grid[4], r0[4], r1[4], r2[4], r3[4];
+};
+static_assert(sizeof(View) == 176, "ViewUniform is 176 bytes");
+
+struct Vol {
+    const uint16_t *tex;
+    int nx, ny, nz;
+    int quant;  // filter-weight fraction: 0 exact, 1 nearest 1/256, 2 truncated 1/256
+};
+
+using f3v = vec3<float>;
+inline f3v v3(float x, float y, float z) { return f3v{x, y, z}; }
+inline f3v vadd(f3v a, f3v b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline f3v vsub(f3v a, f3v b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline f3v vmul(f3v a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+inline float vdot(f3v a, f3v b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline f3v vnorm(f3v a) {
+    const float l = std::sqrt(vdot(a, a));
+    return v3(a.x / l, a.y / l, a.z / l);
+}
+inline float wclamp(float x, float lo, float hi) { return std::fmin(std::fmax(x, lo), hi); }
+inline float wmix(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+inline f3v wmix3(f3v a, f3v b, float t) { return v3(wmix(a.x, b.x, t), wmix(a.y, b.y, t), wmix(a.z, b.z, t)); }
+inline float wfract(float x) { return x - std::floor(x); }
+
+// Colour maps, shaders/volume.wgsl:37-78.
+const float kViridis[11][3] = {{0.267f, 0.005f, 0.329f}, {0.283f, 0.141f, 0.458f}, {0.254f, 0.265f, 0.530f},
+                               {0.207f, 0.372f, 0.553f}, {0.164f, 0.471f, 0.558f}, {0.128f, 0.567f, 0.551f},
+                               {0.135f, 0.659f, 0.518f}, {0.267f, 0.749f, 0.441f}, {0.478f, 0.821f, 0.318f},
+                               {0.741f, 0.873f, 0.150f}, {0.993f, 0.906f, 0.144f}};
+const float kInferno[11][3] = {{0.001f, 0.000f, 0.014f}, {0.078f, 0.044f, 0.214f}, {0.225f, 0.036f, 0.388f},
+                               {0.373f, 0.074f, 0.432f}, {0.522f, 0.128f, 0.420f}, {0.665f, 0.182f, 0.370f},
+                               {0.798f, 0.280f, 0.270f}, {0.902f, 0.413f, 0.144f}, {0.969f, 0.579f, 0.032f},
+                               {0.988f, 0.762f, 0.135f}, {0.988f, 0.998f, 0.645f}};
+const float kSigned[11][3] = {{0.30f, 0.55f, 1.00f}, {0.22f, 0.42f, 0.85f}, {0.15f, 0.30f, 0.66f},
+                              {0.09f, 0.19f, 0.45f}, {0.04f, 0.09f, 0.24f}, {0.02f, 0.02f, 0.03f},
+                              {0.26f, 0.09f, 0.04f}, {0.48f, 0.17f, 0.06f}, {0.72f, 0.29f, 0.08f},
+                              {0.92f, 0.48f, 0.14f}, {1.00f, 0.72f, 0.32f}};
+
+// ramp (shaders/volume.wgsl:80-90)
+inline f3v ramp(float t, int which) {
+    const float x = wclamp(t, 0.0f, 1.0f) * 10.0f;
+    const int i0 = (int)std::floor(x);
+    const int i1 = i0 + 1 < 10 ? i0 + 1 : 10;
+    const float f = x - std::floor(x);
+    const float(*tab)[3] = which == 0 ? kViridis : (which == 1 ? kInferno : kSigned);
+    return wmix3(v3(tab[i0][0], tab[i0][1], tab[i0][2]), v3(tab[i1][0], tab[i1][1], tab[i1][2]), f);
+}
+
+// Trilinear filtering with clamp-to-edge addressing and normalised
+// coordinates: texel space x = u n - 1/2, weights from the fraction.
+inline void tex_sample(const Vol &T, float u, float v, float w, float out[4]) {
+    const float c[3] = {u * (float)T.nx - 0.5f, v * (float)T.ny - 0.5f, w * (float)T.nz - 0.5f};
+    const int n[3] = {T.nx, T.ny, T.nz};
+    int i0[3], i1[3];
+    float a[3];
+    for (int k = 0; k < 3; ++k) {
+        const float fl = std::floor(c[k]);
+        float f = c[k] - fl;
+        if (T.quant == 1) f = std::nearbyint(f * 256.0f) / 256.0f;
+        else if (T.quant == 2) f = std::floor(f * 256.0f) / 256.0f;
+        a[k] = f;
+        const int b = (int)fl;
+        i0[k] = b < 0 ? 0 : (b > n[k] - 1 ? n[k] - 1 : b);
+        i1[k] = b + 1 < 0 ? 0 : (b + 1 > n[k] - 1 ? n[k] - 1 : b + 1);
+    }
+    for (int ch = 0; ch < 4; ++ch) out[ch] = 0.0f;
+    for (int dz = 0; dz < 2; ++dz)
+        for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx) {
+                const float wgt = (dx ? a[0] : 1.0f - a[0]) * (dy ? a[1] : 1.0f - a[1]) * (dz ? a[2] : 1.0f - a[2]);
+                const int x = dx ? i1[0] : i0[0], y = dy ? i1[1] : i0[1], z = dz ? i1[2] : i0[2];
+                const uint16_t *t = T.tex + 4 * (((size_t)z * T.ny + y) * T.nx + x);
+                for (int ch = 0; ch < 4; ++ch) out[ch] += wgt * f16_to_f32(t[ch]);
+            }
+}
+
+// sample_state (shaders/volume.wgsl:115-121)
+inline void sample_state(const View &V, const Vol &T, f3v p, float s[4]) {
+    tex_sample(T, (p.x / V.box[0]) * 0.5f + 0.5f, (p.y / V.box[1]) * 0.5f + 0.5f, (p.z / V.box[2]) * 0.5f + 0.5f, s);
+}
+
+// fs_main (shaders/volume.wgsl:229-381) for the pixel centre (px, py).
+inline f3v fs_main(const View &V, const Vol &T, float px, float py, float ndc_x, float ndc_y) {
+    const f3v ro = v3(V.cam[0], V.cam[1], V.cam[2]);
+    float far4[4];
+    for (int r = 0; r < 4; ++r) far4[r] = V.m[r] * ndc_x + V.m[4 + r] * ndc_y + V.m[8 + r] * 1.0f + V.m[12 + r] * 1.0f;
+    const f3v rd = vnorm(vsub(v3(far4[0] / far4[3], far4[1] / far4[3], far4[2] / far4[3]), ro));
+
+    const float horizon = wclamp(rd.y * 0.5f + 0.5f, 0.0f, 1.0f);
+    f3v color = vmul(wmix3(v3(0.015f, 0.017f, 0.028f), v3(0.045f, 0.055f, 0.085f), horizon), V.r3[2]);
+
+    auto safe_inv = [](float x) {
+        const float s = x < 0.0f ? -1.0f : 1.0f;
+        return s / std::fmax(std::fabs(x), 1e-9f);
+    };
+    const f3v inv_rd = v3(safe_inv(rd.x), safe_inv(rd.y), safe_inv(rd.z));
+    const f3v half = v3(V.box[0], V.box[1], V.box[2]);
+    const f3v t0 = v3((-half.x - ro.x) * inv_rd.x, (-half.y - ro.y) * inv_rd.y, (-half.z - ro.z) * inv_rd.z);
+    const f3v t1 = v3((half.x - ro.x) * inv_rd.x, (half.y - ro.y) * inv_rd.y, (half.z - ro.z) * inv_rd.z);
+    const float tmin_x = std::fmin(t0.x, t1.x), tmin_y = std::fmin(t0.y, t1.y), tmin_z = std::fmin(t0.z, t1.z);
+    const float tmax_x = std::fmax(t0.x, t1.x), tmax_y = std::fmax(t0.y, t1.y), tmax_z = std::fmax(t0.z, t1.z);
+    float t_near = std::fmax(std::fmax(std::fmax(tmin_x, tmin_y), tmin_z), 0.0f);
+    float t_far = std::fmin(std::fmin(tmax_x, tmax_y), tmax_z);
+    if (t_near >= t_far) return color;
+
+    const int clip_axis = (int)V.r1[1];
+    if (clip_axis >= 0) {
+        const float n_axis[3] = {clip_axis == 0 ? 1.0f : 0.0f, clip_axis == 1 ? 1.0f : 0.0f, clip_axis == 2 ? 1.0f : 0.0f};
+        const float plane = V.r1[2] * V.box[clip_axis];
+        const float denom = rd.x * n_axis[0] + rd.y * n_axis[1] + rd.z * n_axis[2];
+        const float dist = plane - (ro.x * n_axis[0] + ro.y * n_axis[1] + ro.z * n_axis[2]);
+        if (std::fabs(denom) < 1e-6f) {
+            if (dist < 0.0f) return color;
+        } else {
+            const float t_plane = dist / denom;
+            if (denom > 0.0f) t_far = std::fmin(t_far, t_plane);
+            else t_near = std::fmax(t_near, t_plane);
+            if (t_near >= t_far) return color;
+        }
+    }
+
+    if (V.r3[1] > 0.5f) {
+        const float w = 0.004f * V.box[3] * V.grid[0];
+        float edge = 0.0f;
+        for (int k = 0; k < 2; ++k) {
+            const f3v p = vadd(ro, vmul(rd, k == 0 ? t_near : t_far));
+            const f3v d = v3(half.x - std::fabs(p.x), half.y - std::fabs(p.y), half.z - std::fabs(p.z));
+            const float median = std::fmax(std::fmin(d.x, d.y), std::fmin(std::fmax(d.x, d.y), d.z));
+            const float st = wclamp((median - 0.0f) / (w - 0.0f), 0.0f, 1.0f);
+            edge = std::fmax(edge, 1.0f - st * st * (3.0f - 2.0f * st));
+        }
+        color = vadd(color, vmul(v3(0.20f, 0.26f, 0.34f), edge));
+    }
+
+    const float cell = V.box[3];
+    const float spc = std::fmax(V.r0[2], 0.25f);
+    float ds = cell / spc;
+    const float span = t_far - t_near;
+    if (span / ds > 2048.0f) ds = span / 2048.0f;
+    const int n_steps = std::min((int)std::ceil(span / ds), 2048);
+
+    // hash12 (shaders/volume.wgsl:136-140) of the pixel centre + the frame offset
+    const float hx = px + V.r3[0], hy = py + V.r3[0];
+    f3v p3 = v3(wfract(hx * 0.1031f), wfract(hy * 0.1031f), wfract(hx * 0.1031f));
+    const float dd = vdot(p3, v3(p3.y + 33.33f, p3.z + 33.33f, p3.x + 33.33f));
+    p3 = v3(p3.x + dd, p3.y + dd, p3.z + dd);
+    const float jitter = wfract((p3.x + p3.y) * p3.z);
+
+    const float iso = V.r0[0], wall_opacity = V.r0[1], exposure = V.r0[3], absorption = V.r2[1];
+    const bool show_iso = V.r2[2] > 0.5f, show_vol = V.r2[3] > 0.5f;
+    f3v accum = v3(0.0f, 0.0f, 0.0f);
+    float alpha = 0.0f;
+    float t = t_near + jitter * ds;
+    float s0[4];
+    sample_state(V, T, vadd(ro, vmul(rd, t_near)), s0);
+    float prev_phi = s0[0];
+    float prev_t = t_near;
+    const f3v l1 = vnorm(v3(0.55f, 0.72f, 0.42f));
+    const f3v l2 = vnorm(v3(-0.5f, -0.2f, -0.7f));
+    for (int i = 0; i < n_steps; ++i) {
+        if (t > t_far || alpha > 0.995f) break;
+        const f3v p = vadd(ro, vmul(rd, t));
+        float s[4];
+        sample_state(V, T, p, s);
+        const float d_prev = prev_phi - iso;
+        const float d_cur = s[0] - iso;
+        if (show_iso && d_prev != 0.0f && d_prev * d_cur <= 0.0f) {
+            const float denom = s[0] - prev_phi;
+            const float frac = std::fabs(denom) > 1e-6f ? (iso - prev_phi) / denom : 0.5f;
+            const float t_hit = wmix(prev_t, t, wclamp(frac, 0.0f, 1.0f));
+            const f3v p_hit = vadd(ro, vmul(rd, t_hit));
+            const float h = V.box[3];
+            float a_[4], b_[4];
+            float g[3];
+            for (int k = 0; k < 3; ++k) {
+                const f3v e = v3(k == 0 ? h : 0.0f, k == 1 ? h : 0.0f, k == 2 ? h : 0.0f);
+                sample_state(V, T, vadd(p_hit, e), a_);
+                sample_state(V, T, vsub(p_hit, e), b_);
+                g[k] = a_[0] - b_[0];
+            }
+            const f3v grad = v3(g[0] / (2.0f * h), g[1] / (2.0f * h), g[2] / (2.0f * h));
+            const f3v n = vnorm(vsub(vmul(grad, -1.0f), vmul(rd, 1e-6f)));
+            float hs[4];
+            sample_state(V, T, p_hit, hs);
+            const float drive = wclamp(hs[1] * 4.0f, 0.0f, 1.0f);
+            const f3v base = wmix3(v3(0.16f, 0.62f, 0.72f), v3(1.00f, 0.72f, 0.28f), drive);
+            const f3v view = vmul(rd, -1.0f);
+            const float diff = std::fmax(vdot(n, l1), 0.0f) + 0.35f * std::fmax(vdot(n, l2), 0.0f);
+            const f3v hh = vnorm(vadd(vadd(l1, view), v3(0.0f, 1e-5f, 0.0f)));
+            const float spec = std::pow(std::fmax(vdot(n, hh), 0.0f), 48.0f);
+            const float fres = std::pow(1.0f - std::fabs(vdot(n, view)), 3.0f);
+            const f3v shaded = vadd(vadd(vmul(base, 0.22f + 0.85f * diff), vmul(v3(1.0f, 1.0f, 1.0f), spec * 0.35f)),
+                                    vmul(vmul(base, fres), 0.9f));
+            const float a = wall_opacity;
+            accum = vadd(accum, vmul(vmul(shaded, 1.0f - alpha), a));
+            alpha = alpha + (1.0f - alpha) * a;
+        }
+        if (show_vol) {
+            // map_field (shaders/volume.wgsl:152-185)
+            const int mode = (int)V.r1[0];
+            const float gain = V.r2[0];
+            int rid = (int)V.r1[3];
+            float mt, mi;
+            if (mode == 0) {
+                const float x = wclamp(s[0], 0.0f, 1.0f);
+                mt = x;
+                mi = x * gain;
+            } else if (mode == 1) {
+                const float x = wclamp(s[1] * gain, 0.0f, 1.0f);
+                mt = x;
+                mi = x;
+            } else if (mode == 2) {
+                const float x = wclamp(s[2] * gain, -1.0f, 1.0f);
+                mt = 0.5f + 0.5f * x;
+                mi = std::fabs(x);
+                rid = 2;
+            } else {
+                const float x = wclamp(s[3] * gain, 0.0f, 1.0f);
+                mt = x;
+                mi = x;
+            }
+            if (mi > 1e-4f) {
+                const float weight = mi * mi;
+                const float a = 1.0f - std::exp(-absorption * weight * ds);
+                const f3v emit = vmul(ramp(mt, rid), exposure);
+                accum = vadd(accum, vmul(vmul(emit, 1.0f - alpha), a));
+                alpha = alpha + (1.0f - alpha) * a;
+            }
+        }
+        prev_phi = s[0];
+        prev_t = t;
+        t = t + ds;
+    }
+    return vadd(vmul(color, 1.0f - alpha), accum);
+}
+
+void render_all(const View &V, const Vol &T, int width, int height, uint8_t *out) {
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int py = 0; py < height; ++py)
+        for (int px = 0; px < width; ++px) {
+            const float fx = (float)px + 0.5f, fy = (float)py + 0.5f;
+            const float ndc_x = fx / (float)width * 2.0f - 1.0f;
+            const float ndc_y = 1.0f - fy / (float)height * 2.0f;
+            f3v c = fs_main(V, T, fx, fy, ndc_x, ndc_y);
+            c = v3(c.x / (1.0f + c.x), c.y / (1.0f + c.y), c.z / (1.0f + c.z));
+            const float g = 1.0f / 2.2f;
+            const float rgb[3] = {std::pow(std::fmax(c.x, 0.0f), g), std::pow(std::fmax(c.y, 0.0f), g),
+                                  std::pow(std::fmax(c.z, 0.0f), g)};
+            uint8_t *o = out + 4 * ((size_t)py * width + px);
+            for (int k = 0; k < 3; ++k) o[k] = (uint8_t)std::nearbyint(wclamp(rgb[k], 0.0f, 1.0f) * 255.0f);
+            o[3] = 255;
+        }
+}
+
 }  // namespace
 
 extern "C" {
@@ -532,6 +855,24 @@ void oracle_set_threads(int n) {
 
 ORACLE_API(float, f32)
 ORACLE_API(double, f64)
+
+void oracle_vis_f32(const SimParams<float> *P, const float *field, const float *fluid, const float *prim,
+                    uint16_t *out) {
+    vis_all(*P, field, fluid, prim, out);
+}
+void oracle_vis_f64(const SimParams<double> *P, const double *field, const double *fluid, const double *prim,
+                    uint16_t *out) {
+    vis_all(*P, field, fluid, prim, out);
+}
+// One frame of the volume renderer over half4 texels `tex` (nx*ny*nz).
+void oracle_render(const float *view44, const uint16_t *tex, int nx, int ny, int nz, int width, int height,
+                   int quant, uint8_t *out) {
+    View V;
+    std::memcpy(&V, view44, sizeof(View));
+    const Vol T{tex, nx, ny, nz, quant};
+    render_all(V, T, width, height, out);
+}
+uint16_t oracle_f32_to_f16(float x) { return f32_to_f16(x); }
 
 double oracle_tanh_f64(double x) { return oracle_tanh(x); }
 float oracle_tanh_f32(float x) { return oracle_tanh_r(x); }

@@ -74,6 +74,11 @@ def lib() -> ctypes.CDLL:
         L.oracle_tanh_f32.argtypes = [ctypes.c_float]
         L.oracle_tanh_f32.restype = ctypes.c_float
         L.oracle_set_threads.argtypes = [ctypes.c_int]
+        L.oracle_vis_f32.argtypes = [P] * 5
+        L.oracle_vis_f64.argtypes = [P] * 5
+        L.oracle_render.argtypes = [P, P] + [ctypes.c_int] * 6 + [P]
+        L.oracle_f32_to_f16.argtypes = [ctypes.c_float]
+        L.oracle_f32_to_f16.restype = ctypes.c_uint16
         _lib = L
     return _lib
 
@@ -91,6 +96,24 @@ def expf(x) -> np.float32:
 
 def logf(x) -> np.float32:
     return f32(_libm.logf(float(f32(x))))
+
+
+def render(view: np.ndarray, tex: np.ndarray, width: int, height: int, quant: int = 1) -> np.ndarray:
+    """fs_main of shaders/volume.wgsl over the half4 texels `tex` ((nz, ny,
+    nx, 4) uint16) with the 176-byte view uniform `view` (44 float32):
+    (height, width, 4) uint8.  `quant` sets the trilinear weights' fraction:
+    0 exact, 1 rounded to 1/256, 2 truncated to 1/256."""
+    view = np.ascontiguousarray(view, dtype=np.float32)
+    tex = np.ascontiguousarray(tex, dtype=np.uint16)
+    assert view.size == 44 and tex.ndim == 4 and tex.shape[3] == 4
+    nz, ny, nx, _ = tex.shape
+    out = np.zeros((height, width, 4), dtype=np.uint8)
+    lib().oracle_render(_ptr(view), _ptr(tex), nx, ny, nz, width, height, quant, _ptr(out))
+    return out
+
+
+def f32_to_f16(x) -> int:
+    return int(lib().oracle_f32_to_f16(float(f32(x))))
 
 
 # ---------------------------------------------------------------------------
@@ -379,6 +402,19 @@ class OracleSim:
 
     def remaining_bubbles(self) -> int:
         return max(len(self.schedule) - self.next_event, 0)
+
+    # record_visualisation (src/gpu/sim.rs:918-942): primitives pass + vis pass
+    def visualise(self) -> np.ndarray:
+        """The vis texture of the current slot as (nz, ny, nx, 4) uint16
+        (binary16 bits of phi/phi_b, |v|, T/T_ref - 1, (E+p)v^2/e_ref)."""
+        L = lib()
+        getattr(L, f"oracle_primitives_{self.sfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
+                                                    _ptr(self.fluid[self.cur]), _ptr(self.prim))
+        nx, ny, nz = self.grid
+        out = np.zeros((nz, ny, nx, 4), dtype=np.uint16)
+        getattr(L, f"oracle_vis_{self.sfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
+                                             _ptr(self.fluid[self.cur]), _ptr(self.prim), _ptr(out))
+        return out
 
     # record_visualisation's primitives pass + reduce (src/gpu/sim.rs:918-1010)
     def diagnostics(self) -> dict:

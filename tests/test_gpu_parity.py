@@ -216,9 +216,9 @@ def test_nonfinite_state_is_reported(bubble, gpu):
 @pytest.mark.parametrize("path", ["fused", "fused_sync"])
 def test_tile_shapes_agree(bubble, gpu, golden, path):
     """Every z chunking of one kernel instantiation gives identical bits; the
-    fast mode's two tile heights are separate instantiations whose FMA
-    contraction may differ, so they agree within the fast-path bar, 1e-5
-    relative (measured: 1.6e-6 after 5 steps of this shocked case)."""
+    fast mode's two tile heights are separate instantiations whose FMA contraction may differ, so they agree
+    within the fast-path bar, 1e-5 relative (measured: 1.6e-6 after 5 steps
+    of this shocked case)."""
     case = "tile_partial"
     grid = golden[f"{case}_grid"]
     f0, u0 = golden[f"{case}_f32_field0"], golden[f"{case}_f32_fluid0"]
