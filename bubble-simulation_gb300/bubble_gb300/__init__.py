@@ -19,7 +19,7 @@ from ._lib import BubbleError, check, load
 __all__ = ["Model", "SimulationSpec", "Simulation", "Diagnostics", "make_schedule", "derived",
            "validate_model", "stage_slots", "rk3_coefficients", "lattice_bytes", "max_cubic_size",
            "vram_query", "vram_available", "lattice_budget", "BubbleError", "load", "render_settings", "camera",
-           "render_view", "write_png"]
+           "render_view", "write_png", "checkpoint_spec"]
 
 
 @dataclass
@@ -121,6 +121,12 @@ class SimulationSpec:
         return _lib.Spec(self.model.c(), (ctypes.c_uint32 * 3)(*self.grid), _lib.NUCLEATION[self.nucleation],
                          self.bubbles, self.nucleation_duration, self.seed, _lib.PRECISION[self.precision],
                          _lib.MATH[self.math])
+
+    @classmethod
+    def from_c(cls, c: _lib.Spec) -> "SimulationSpec":
+        inv = lambda d, v: next(k for k, x in d.items() if x == v)  # noqa: E731
+        return cls(Model.from_c(c.model), tuple(c.grid), inv(_lib.NUCLEATION, c.nucleation), c.bubbles,
+                   c.nucleation_duration, c.seed, inv(_lib.PRECISION, c.precision), inv(_lib.MATH, c.math))
 
 
 @dataclass
@@ -282,6 +288,26 @@ class Simulation:
         fn = self._L.bubble_load_state_f64 if self._dtype == np.float64 else self._L.bubble_load_state
         check(fn(self._h, field.ctypes.data, fluid.ctypes.data))
 
+    # -- checkpoint and resume (include/bubble_checkpoint.h) ------------------
+    def save_checkpoint(self, path: str):
+        check(self._L.bubble_checkpoint_save(self._h, str(path).encode()))
+
+    def restore_checkpoint(self, path: str):
+        check(self._L.bubble_checkpoint_restore(self._h, str(path).encode()))
+
+    @classmethod
+    def from_checkpoint(cls, path: str, precision: str | None = None, math: str | None = None) -> "Simulation":
+        """A simulation created with the checkpoint's spec (optionally another
+        arithmetic of the same FP32/FP64 layout) and restored from it."""
+        spec = checkpoint_spec(path)
+        if precision is not None:
+            spec.precision = precision
+        if math is not None:
+            spec.math = math
+        sim = cls(spec)
+        sim.restore_checkpoint(path)
+        return sim
+
     # -- visualisation (include/bubble_render.h) ------------------------------
     def visualise(self):
         """record_visualisation (src/gpu/sim.rs:918-942) into the vis texture."""
@@ -308,6 +334,13 @@ class Simulation:
         """capture::render_to_png (src/capture.rs:19-117)."""
         settings = settings or render_settings()
         check(self._L.bubble_render_png(self._h, ctypes.byref(settings), size[0], size[1], str(path).encode()))
+
+
+def checkpoint_spec(path: str) -> SimulationSpec:
+    """The SimulationSpec stored in a checkpoint file (no device work)."""
+    c = _lib.Spec()
+    check(load().bubble_checkpoint_spec(str(path).encode(), ctypes.byref(c)))
+    return SimulationSpec.from_c(c)
 
 
 def render_settings(field: str | None = None) -> _lib.RenderSettings:

@@ -25,7 +25,7 @@ ERR_TIMEOUT = -6
 SEED_CRITICAL = 0
 SEED_CELLS = 1
 NUCLEATION = {"simultaneous": 0, "exponential": 1, "centre": 2, "uniform": 3}
-PRECISION = {"single": 0, "mixed": 1, "double": 2}
+PRECISION = {"single": 0, "mixed": 1, "double": 2, "perturbation": 3}
 MATH = {"fast": 0, "strict": 1}
 PATH_FUSED = 0
 PATH_REFERENCE = 1
@@ -231,6 +231,11 @@ SIGNATURES = [
     ("bubble_render_png", ctypes.c_int, [_P, ctypes.POINTER(RenderSettings), ctypes.c_uint32, ctypes.c_uint32,
                                          ctypes.c_char_p]),
     ("bubble_write_png", ctypes.c_int, [ctypes.c_char_p, _P, ctypes.c_uint32, ctypes.c_uint32]),
+    # bubble_checkpoint.h
+    ("bubble_checkpoint_save", ctypes.c_int, [_P, ctypes.c_char_p]),
+    ("bubble_checkpoint_restore", ctypes.c_int, [_P, ctypes.c_char_p]),
+    ("bubble_checkpoint_spec", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Spec)]),
+    ("bubble_checkpoint_open", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_P)]),
 ]
 
 _lib = None

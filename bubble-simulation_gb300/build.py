@@ -56,7 +56,7 @@ KERNEL_UNITS = {
     "render.cu": ["--fmad=false"],
 }
 HOST_UNITS = ["physics.cpp", "simulation.cpp", "capi.cpp", "tma.cpp", "batch.cpp", "capi_batch.cpp", "server.cpp",
-              "render_host.cpp"]
+              "render_host.cpp", "checkpoint.cpp"]
 CLI_UNITS = ["headless.cpp"]
 HEADERS = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
 

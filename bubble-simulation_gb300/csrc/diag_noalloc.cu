@@ -115,7 +115,7 @@ int bubble_diagnostics_noalloc(const void *field, const void *fluid, const uint3
             return fail(BUBBLE_ERR_INVALID, "grid axis " + std::to_string(a) + " is " +
                                                 std::to_string(grid[a]) + "; accepted axes are 8..2048");
     if (precision < BUBBLE_PRECISION_SINGLE || precision > BUBBLE_PRECISION_DOUBLE)
-        return fail(BUBBLE_ERR_INVALID, "unknown precision");
+        return fail(BUBBLE_ERR_INVALID, "precision must be SINGLE, MIXED or DOUBLE");
     const std::string msg = bubble::validate_model(*model);
     if (!msg.empty()) return fail(BUBBLE_ERR_INVALID, msg);
     const uint64_t cells = (uint64_t)grid[0] * grid[1] * grid[2];

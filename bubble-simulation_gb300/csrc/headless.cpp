@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/bubble.h"
+#include "../../include/bubble_checkpoint.h"
 #include "../../include/bubble_render.h"
 
 namespace {
@@ -38,6 +39,7 @@ struct Args {
     unsigned long long report_every = 0;
     std::string screenshot;
     uint32_t screenshot_size[2] = {1280, 960};
+    std::string save_checkpoint, resume;
     int field = BUBBLE_FIELD_KINETIC;
     int precision = BUBBLE_PRECISION_SINGLE;
     int math = BUBBLE_MATH_FAST;
@@ -107,12 +109,15 @@ void usage() {
         "  --steps-per-frame N       steps per frame [default: 2]\n"
         "  --headless N              run N steps and print diagnostics\n"
         "  --report-every K          report interval [default: max(N/20, 1)]\n"
-        "  --precision MODE          single|mixed|double [default: single]\n"
+        "  --precision MODE          single|mixed|double|perturbation [default: single]\n"
         "  --math MODE               fast|strict [default: fast]\n"
         "  --field F                 phi|speed|temperature|kinetic, for --screenshot [default: kinetic]\n"
         "  --screenshot PATH         render one frame to this PNG and exit\n"
         "  --screenshot-size WxH     resolution of --screenshot [default: 1280x960]\n"
-        "  --no-vsync                accepted for compatibility; no effect headless\n");
+        "  --no-vsync                accepted for compatibility; no effect headless\n"
+        "  --save-checkpoint PATH    write the final state to a checkpoint file\n"
+        "  --resume PATH             continue from a checkpoint (its grid, model and schedule;\n"
+        "                            --precision/--math must match its FP32/FP64 layout)\n");
 }
 
 bool parse_size(const std::string &s, uint32_t out[2], std::string &msg);
@@ -173,7 +178,9 @@ Args parse(int argc, char **argv) {
             std::string msg;
             if (!parse_size(v, a.screenshot_size, msg))
                 die("invalid value '" + v + "' for '--screenshot-size <SCREENSHOT_SIZE>': " + msg);
-        } else if (f == "--field") {
+        } else if (f == "--save-checkpoint") a.save_checkpoint = next();
+        else if (f == "--resume") a.resume = next();
+        else if (f == "--field") {
             const std::string m = next();
             if (m == "phi") a.field = BUBBLE_FIELD_PHI;
             else if (m == "speed") a.field = BUBBLE_FIELD_SPEED;
@@ -187,6 +194,7 @@ Args parse(int argc, char **argv) {
             if (m == "single") a.precision = BUBBLE_PRECISION_SINGLE;
             else if (m == "mixed") a.precision = BUBBLE_PRECISION_MIXED;
             else if (m == "double") a.precision = BUBBLE_PRECISION_DOUBLE;
+            else if (m == "perturbation") a.precision = BUBBLE_PRECISION_PERTURBATION;
             else die("invalid value '" + m + "' for '--precision'");
         } else if (f == "--math") {
             const std::string m = next();
@@ -306,15 +314,26 @@ int run(const Args &a, unsigned long long steps, unsigned long long every) {
     spec.precision = a.precision;
     spec.math = a.math;
     bubble_sim *sim = nullptr;
-    if (bubble_create(&spec, &sim) != BUBBLE_OK)
+    if (!a.resume.empty()) {
+        // the checkpoint's grid, model, schedule and clock; this run's arithmetic
+        bubble_spec saved;
+        if (bubble_checkpoint_spec(a.resume.c_str(), &saved) != BUBBLE_OK) die(bubble_last_error(), 1);
+        saved.precision = spec.precision;
+        saved.math = spec.math;
+        spec = saved;
+        if (bubble_create(&spec, &sim) != BUBBLE_OK)
+            die(std::string("failed to create the simulation: ") + bubble_last_error(), 1);
+        if (bubble_checkpoint_restore(sim, a.resume.c_str()) != BUBBLE_OK) die(bubble_last_error(), 1);
+    } else if (bubble_create(&spec, &sim) != BUBBLE_OK) {
         die(std::string("failed to create the simulation: ") + bubble_last_error(), 1);
+    }
     bubble_vram_info vi;
     if (bubble_vram_query(&vi) == BUBBLE_OK)
         std::printf("adapter: CUDA device (%.1f GB)\n", (double)vi.capacity / 1e9);
     bubble_derived d;
     bubble_model_derived(&spec.model, &d);
-    std::printf("lattice %ux%ux%u = %.2f M cells | %.2f GB | dt = %.3f\n", a.grid[0], a.grid[1],
-                a.grid[2], (double)bubble_cell_count(sim) / 1e6,
+    std::printf("lattice %ux%ux%u = %.2f M cells | %.2f GB | dt = %.3f\n", spec.grid[0], spec.grid[1],
+                spec.grid[2], (double)bubble_cell_count(sim) / 1e6,
                 (double)bubble_device_memory_bytes(sim) / 1e9, (double)d.dt);
     std::printf("wall %.2f cells | R_c %.1f cells | sigma %.4f | eps %.4f | e_ref %.4f\n",
                 (double)d.wall_width, (double)d.critical_radius, (double)d.surface_tension,
@@ -354,7 +373,8 @@ int run(const Args &a, unsigned long long steps, unsigned long long every) {
         const float cells = (float)bubble_cell_count(sim);
         const float volume = dg.broken_fraction * cells;
         const float r_eq = std::cbrt(volume * 3.0f / (4.0f * 3.14159265358979323846f));
-        std::printf("%10llu %10.1f %9.2f%% %10.1f %11.4f %s %s\n", done, (double)bubble_time(sim),
+        std::printf("%10llu %10.1f %9.2f%% %10.1f %11.4f %s %s\n", (unsigned long long)bubble_steps(sim),
+                    (double)bubble_time(sim),
                     100.0 * (double)dg.broken_fraction, (double)r_eq, (double)dg.max_velocity,
                     pad_left(rust_exp3(dg.kinetic_fraction), 11).c_str(), pad_left(ratio, 10).c_str());
         std::fflush(stdout);
@@ -365,6 +385,15 @@ int run(const Args &a, unsigned long long steps, unsigned long long every) {
         const double cell_steps = (double)steps * (double)bubble_cell_count(sim);
         std::printf("\n%llu steps in %.2f s  (%.1f steps/s, %.2f G cell-updates/s)\n", steps, elapsed,
                     (double)steps / elapsed, cell_steps / elapsed / 1e9);
+    }
+    if (!a.save_checkpoint.empty()) {
+        if (bubble_checkpoint_save(sim, a.save_checkpoint.c_str()) != BUBBLE_OK) {
+            const std::string msg = bubble_last_error();
+            bubble_destroy(sim);
+            die(msg, 1);
+        }
+        std::printf("checkpoint %s (step %llu)\n", a.save_checkpoint.c_str(),
+                    (unsigned long long)bubble_steps(sim));
     }
     if (!a.screenshot.empty()) {
         // render_to_png (src/capture.rs:19-117) of the current state

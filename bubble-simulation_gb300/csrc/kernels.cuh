@@ -234,7 +234,7 @@ struct FusedLayout {
     static constexpr size_t bytes = o_phi + sizeof(R) * PHI_RING * PC;
 };
 
-template <typename R, bool FAST, bool MIXED, int TX, int TY>
+template <typename R, bool FAST, int MIXED, int TX, int TY>
 __global__ void __launch_bounds__(TX *(TY + 1))
     stage_fused_kernel(StageArgs<R> A, LatticeParams<R> P, int lz) {
     using L = FusedLayout<R, TX, TY>;
@@ -481,7 +481,7 @@ BUBBLE_DEV double warp_sum(double v) {
     return v;
 }
 
-template <typename R, bool MIXED>
+template <typename R, int MIXED>
 __global__ void __launch_bounds__(kDiagThreads)
     diag_kernel(const V2<R> *__restrict__ field, const V4<R> *__restrict__ fluid,
                 LatticeParams<R> P, DiagPartial *__restrict__ partials,
@@ -522,12 +522,16 @@ __global__ void __launch_bounds__(kDiagThreads)
             grad2 = grad2 + d * d;
         }
         const V4<R> u = fluid[i];
+        // In the perturbation form e_lab is max(E, e_floor) - e_bg: the sums of
+        // e_total and e_lab then miss N e_bg, which the host adds in FP64.
         const R e_lab = vmax(u.x, P.e_floor);
         const V4<R> q = recover<R, false, MIXED>(u, P);
         const R v2 = q.x * q.x + q.y * q.y + q.z * q.z;
         const R e_total = R(0.5) * pi * pi + R(0.5) * grad2 + potential(phi, P) + e_lab;
         const R broken = phi > R(0.5) * P.phi_b ? R(1.0) : R(0.0);
-        const R kinetic = (e_lab + q.w) * v2;
+        R kinetic;
+        if constexpr (MIXED == kPert) kinetic = ((e_lab + q.w) + (P.e_bg + P.p_bg)) * v2;
+        else kinetic = (e_lab + q.w) * v2;
         acc[0] += (double)e_total;
         acc[1] += (double)broken;
         acc[2] += (double)kinetic;

@@ -28,16 +28,17 @@ namespace bubble {
 namespace launch {
 
 cudaError_t stage_v2_f32_fast(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
-                              bool mixed, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
+                              int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
     using namespace launch_detail;
     if (shape.tx != 32) return cudaErrorInvalidValue;
     if (shape.ty == 8) {
-        if (mixed) return stage_v2<float, true, true, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-        return stage_v2<float, true, false, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+        if (mode == dev::kPert) return stage_v2<float, true, dev::kPert, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+        if (mode == dev::kMixed) return stage_v2<float, true, dev::kMixed, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+        return stage_v2<float, true, dev::kPlain, 8>(A, P, shape.lz, maps, tma_ok, status, s);
     }
-    if (shape.ty == 4) {
-        if (mixed) return stage_v2<float, true, true, 4>(A, P, shape.lz, maps, tma_ok, status, s);
-        return stage_v2<float, true, false, 4>(A, P, shape.lz, maps, tma_ok, status, s);
+    if (shape.ty == 4 && mode != dev::kPert) {
+        if (mode == dev::kMixed) return stage_v2<float, true, dev::kMixed, 4>(A, P, shape.lz, maps, tma_ok, status, s);
+        return stage_v2<float, true, dev::kPlain, 4>(A, P, shape.lz, maps, tma_ok, status, s);
     }
     return cudaErrorInvalidValue;
 }

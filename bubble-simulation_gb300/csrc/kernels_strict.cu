@@ -33,10 +33,11 @@ cudaError_t stage_fused_f32_strict(const StageArgs<float> &A, const LatticeParam
     return stage_fused<float, false, false, 8>(A, P, shape.lz, s);
 }
 cudaError_t diag_f32(const V2<float> *field, const V4<float> *fluid,
-                     const LatticeParams<float> &P, bool mixed, void *partials,
+                     const LatticeParams<float> &P, int mode, void *partials,
                      unsigned int *ticket, DiagResult *out, cudaStream_t s) {
-    if (mixed) return diag<float, true>(field, fluid, P, partials, ticket, out, s);
-    return diag<float, false>(field, fluid, P, partials, ticket, out, s);
+    if (mode == dev::kPert) return diag<float, dev::kPert>(field, fluid, P, partials, ticket, out, s);
+    if (mode == dev::kMixed) return diag<float, dev::kMixed>(field, fluid, P, partials, ticket, out, s);
+    return diag<float, dev::kPlain>(field, fluid, P, partials, ticket, out, s);
 }
 
 size_t diag_partials_bytes() { return sizeof(dev::DiagPartial) * dev::kDiagMaxBlocks; }
@@ -65,11 +66,12 @@ size_t v2_smem_bytes(int precision_double, int ty) {
     return ty == 4 ? dev::V2Layout<float, 4>::bytes : dev::V2Layout<float, 8>::bytes;
 }
 cudaError_t stage_v2_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
-                                bool mixed, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
+                                int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
     using namespace launch_detail;
     if (shape.tx != 32 || shape.ty != 8) return cudaErrorInvalidValue;
-    if (mixed) return stage_v2<float, false, true, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-    return stage_v2<float, false, false, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+    if (mode == dev::kPert) return stage_v2<float, false, dev::kPert, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+    if (mode == dev::kMixed) return stage_v2<float, false, dev::kMixed, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+    return stage_v2<float, false, dev::kPlain, 8>(A, P, shape.lz, maps, tma_ok, status, s);
 }
 
 }  // namespace launch

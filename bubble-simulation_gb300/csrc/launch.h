@@ -36,8 +36,9 @@ cudaError_t stage_ref_f32(const StageArgs<float> &A, const V4<float> *prim,
                           const LatticeParams<float> &P, cudaStream_t s);
 cudaError_t stage_fused_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P,
                                    TileShape shape, bool mixed, cudaStream_t s);
+// `mode`: 0 plain, 1 mixed, 2 perturbation form (physics.cuh kPlain/kMixed/kPert).
 cudaError_t diag_f32(const V2<float> *field, const V4<float> *fluid,
-                     const LatticeParams<float> &P, bool mixed, void *partials,
+                     const LatticeParams<float> &P, int mode, void *partials,
                      unsigned int *ticket, DiagResult *out, cudaStream_t s);
 
 // ---- FP32 (fast translation unit: FMA, approximate rcp/sqrt) ------------
@@ -68,10 +69,11 @@ int diag_blocks_for(uint64_t cells);
 // whether they are valid; bit 0 of *status is set if a bounded wait expired.
 bool v2_shape_supported(int precision_double, int ty);
 size_t v2_smem_bytes(int precision_double, int ty);
+// `mode` as for diag_f32; the perturbation form is built for ty = 8 only.
 cudaError_t stage_v2_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
-                                bool mixed, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
+                                int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
 cudaError_t stage_v2_f32_fast(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
-                              bool mixed, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
+                              int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
 cudaError_t stage_v2_f64(const StageArgs<double> &A, const LatticeParams<double> &P, TileShape shape,
                          const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
 

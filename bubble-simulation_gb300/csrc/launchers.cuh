@@ -83,7 +83,7 @@ cudaError_t stage_ref(const StageArgs<R> &A, const V4<R> *prim, const LatticePar
     return cudaGetLastError();
 }
 
-template <typename R, bool FAST, bool MIXED, int TY>
+template <typename R, bool FAST, int MIXED, int TY>
 cudaError_t stage_fused(const StageArgs<R> &A, const LatticeParams<R> &P, int lz, cudaStream_t s) {
     constexpr int TX = 32;
     using L = dev::FusedLayout<R, TX, TY>;
@@ -98,7 +98,7 @@ cudaError_t stage_fused(const StageArgs<R> &A, const LatticeParams<R> &P, int lz
     return cudaGetLastError();
 }
 
-template <typename R, bool FAST, bool MIXED, int TY>
+template <typename R, bool FAST, int MIXED, int TY>
 cudaError_t stage_v2(const StageArgs<R> &A, const LatticeParams<R> &P, int lz, const StageMaps &maps, int tma_ok,
                      int *status, cudaStream_t s) {
     using L = dev::V2Layout<R, TY>;
@@ -113,7 +113,7 @@ cudaError_t stage_v2(const StageArgs<R> &A, const LatticeParams<R> &P, int lz, c
     return cudaGetLastError();
 }
 
-template <typename R, bool MIXED>
+template <typename R, int MIXED>
 cudaError_t diag(const V2<R> *field, const V4<R> *fluid, const LatticeParams<R> &P,
                  void *partials, unsigned int *ticket, DiagResult *out, cudaStream_t s) {
     const uint64_t n = (uint64_t)P.nx * P.ny * P.nz;

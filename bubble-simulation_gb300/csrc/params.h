@@ -32,6 +32,10 @@ struct LatticeParams {
     R dx, inv_dx, eta, lambda;
     R phi_b, m2, delta, wall_width;
     R p_floor, e_floor, z_max, e_ref;
+    // Perturbation form: the background subtracted from the stored energy
+    // (e_bg = e_ref) and from the pressure (p_bg = e_bg / 3); both 0, and the
+    // floors unshifted, for the other forms.
+    R e_bg, p_bg;
 };
 
 // One SSP-RK3 stage: U_out = a0 U^n + a1 (U_in + dt L(U_in))

@@ -172,14 +172,97 @@ BUBBLE_DEV V4<float> prim_from_cons_f64(const V4<float> &u, const LatticeParams<
     return V4<float>{(float)(zx / s), (float)(zy / s), (float)(zz / s), (float)p};
 }
 
-template <typename R, bool FAST, bool MIXED>
-BUBBLE_DEV V4<R> recover(const V4<R> &u, const LatticeParams<R> &P) {
-    V4<R> q = prim_from_cons<R, FAST>(u, P);
-    if constexpr (MIXED) {
-        const R v2 = q.x * q.x + q.y * q.y + q.z * q.z;
-        if (v2 > R(8.0) / R(9.0)) q = prim_from_cons_f64(u, P);
+// ---------------------------------------------------------------------------
+//  Perturbation form: the fluid energy is stored as E - e_bg (e_bg = e_ref)
+// ---------------------------------------------------------------------------
+// For weak transitions the fluid's departure from the background is a small
+// signal on an O(1) E, and FP32 totals lose its digits.  Storing E - e_bg
+// keeps them.  p = (E^2 - Z^2) / (E + s), s = sqrt(4E^2 - 3Z^2), equals
+// E/3 - Z^2 / (s + 2E) exactly, so with p_bg = e_bg/3
+//     p - p_bg = (E - e_bg)/3 - Z^2 / (s + 2E),
+// in which the background cancels analytically; E itself is needed only in
+// the small Z^2 term and in E + p.  The primitive's w component is p - p_bg,
+// and the floors in LatticeParams hold e_floor - e_bg and p_floor - p_bg.
+template <typename R, bool FAST>
+BUBBLE_DEV V4<R> prim_from_cons_pert(const V4<R> &u, const LatticeParams<R> &P) {
+    const R de = vmax(u.x, P.e_floor);
+    const R e_lab = P.e_bg + de;
+    R zx = u.y, zy = u.z, zz = u.w;
+    const R zcap = P.z_max * e_lab;
+    if constexpr (FAST) {
+        const R z2raw = zx * zx + zy * zy + zz * zz;
+        if (z2raw > zcap * zcap) {
+            const R sc = zcap * rsqrt_approx(z2raw);
+            zx *= sc;
+            zy *= sc;
+            zz *= sc;
+        }
+        const R z2 = zx * zx + zy * zy + zz * zz;
+        const R sq = sqrt_approx(vmax(R(4.0) * e_lab * e_lab - R(3.0) * z2, R(0.0)));
+        R dp = de * R(1.0 / 3.0) - z2 * rcp_approx(sq + R(2.0) * e_lab);
+        dp = vmax(dp, P.p_floor);
+        const R inv = rcp_approx(vmax(e_lab + P.p_bg + dp, R(1e-30)));
+        return V4<R>{zx * inv, zy * inv, zz * inv, dp};
+    } else {
+        const R zlen = sqrt(zx * zx + zy * zy + zz * zz);
+        if (zlen > zcap) {
+            const R sc = zcap / vmax(zlen, R(1e-30));
+            zx = zx * sc;
+            zy = zy * sc;
+            zz = zz * sc;
+        }
+        const R z2 = zx * zx + zy * zy + zz * zz;
+        const R sq = sqrt(vmax(R(4.0) * e_lab * e_lab - R(3.0) * z2, R(0.0)));
+        R dp = de / R(3.0) - z2 / (sq + R(2.0) * e_lab);
+        dp = vmax(dp, P.p_floor);
+        const R d = vmax(e_lab + P.p_bg + dp, R(1e-30));
+        return V4<R>{zx / d, zy / d, zz / d, dp};
     }
-    return q;
+}
+
+// FP64 recovery of one FP32 cell in the perturbation form (gamma > 3).
+BUBBLE_DEV V4<float> prim_from_cons_pert_f64(const V4<float> &u, const LatticeParams<float> &P) {
+    const double de = fmax((double)u.x, (double)P.e_floor);
+    const double e_lab = (double)P.e_bg + de;
+    double zx = u.y, zy = u.z, zz = u.w;
+    const double zcap = (double)P.z_max * e_lab;
+    const double zlen = sqrt(zx * zx + zy * zy + zz * zz);
+    if (zlen > zcap) {
+        const double sc = zcap / fmax(zlen, 1e-30);
+        zx *= sc;
+        zy *= sc;
+        zz *= sc;
+    }
+    const double z2 = zx * zx + zy * zy + zz * zz;
+    const double sq = sqrt(fmax(4.0 * e_lab * e_lab - 3.0 * z2, 0.0));
+    double dp = de / 3.0 - z2 / (sq + 2.0 * e_lab);
+    dp = fmax(dp, (double)P.p_floor);
+    const double d = fmax(e_lab + (double)P.p_bg + dp, 1e-30);
+    return V4<float>{(float)(zx / d), (float)(zy / d), (float)(zz / d), (float)dp};
+}
+
+// Arithmetic forms of a lattice (the MODE parameter of the kernels):
+// plain; mixed = FP64 primitive recovery where the Lorentz factor exceeds 3;
+// perturbation = mixed, with E stored as E - e_bg.
+constexpr int kPlain = 0, kMixed = 1, kPert = 2;
+
+template <typename R, bool FAST, int MODE>
+BUBBLE_DEV V4<R> recover(const V4<R> &u, const LatticeParams<R> &P) {
+    if constexpr (MODE == kPert) {
+        V4<R> q = prim_from_cons_pert<R, FAST>(u, P);
+        if constexpr (sizeof(R) == 4) {
+            const R v2 = q.x * q.x + q.y * q.y + q.z * q.z;
+            if (v2 > R(8.0) / R(9.0)) q = prim_from_cons_pert_f64(u, P);
+        }
+        return q;
+    } else {
+        V4<R> q = prim_from_cons<R, FAST>(u, P);
+        if constexpr (MODE == kMixed) {
+            const R v2 = q.x * q.x + q.y * q.y + q.z * q.z;
+            if (v2 > R(8.0) / R(9.0)) q = prim_from_cons_f64(u, P);
+        }
+        return q;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -266,10 +349,14 @@ struct FaceSide {
     R lm, lp;    // eos_wave_speeds
 };
 
-template <int AXIS, typename R, bool FAST>
-BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2) {
+// PERT: q.w is p - p_bg, the energy component of u is E - e_bg = w v^2 + 3 (p - p_bg)
+// (w = 4p W^2, e_bg = 3 p_bg), and the momentum flux carries p - p_bg: the
+// constant p_bg would cancel in every flux difference.
+template <int AXIS, typename R, bool FAST, bool PERT = false>
+BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2, R p_bg) {
     FaceSide<R> s;
     const R vx = q.x, vy = q.y, vz = q.z, p = q.w;
+    const R pf = PERT ? p_bg + p : p;  // the full pressure
     const R vd = comp<AXIS>(q);
     const R v2 = vmin(vx * vx + vy * vy + vz * vz, zmax2);
     const R cs2 = R(1.0) / R(3.0);  // eos_sound_speed2 (eos.wgsl:50-53)
@@ -277,10 +364,10 @@ BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2) {
         // 1 - vd^2 - cs2 (v^2 - vd^2) = 1 - (2/3) vd^2 - v^2/3 for cs2 = 1/3;
         // E + p = w W^2, so the energy flux is w vd.
         const R om = R(1.0) - v2;
-        const R w = (R(4.0) * p) * rcp_approx(om);
+        const R w = (R(4.0) * pf) * rcp_approx(om);
         {
             const float2 uzw = p_mul(bc2(w), make_float2(vy, vz));
-            s.u = V4<R>{w - p, w * vx, uzw.x, uzw.y};
+            s.u = V4<R>{PERT ? w * v2 + R(3.0) * p : w - p, w * vx, uzw.x, uzw.y};
         }
         const R inv_den = rcp_approx(R(1.0) - v2 * cs2);
         const R tt = R(1.0) - (R(2.0) / R(3.0)) * (vd * vd) - cs2 * v2;
@@ -296,8 +383,8 @@ BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2) {
         if constexpr (AXIS == 2) s.f.w = s.f.w + p;
         return s;
     } else {
-        const R w = R(4.0) * p / (R(1.0) - v2);
-        s.u = V4<R>{w - p, w * vx, w * vy, w * vz};
+        const R w = R(4.0) * pf / (R(1.0) - v2);
+        s.u = V4<R>{PERT ? w * v2 + R(3.0) * p : w - p, w * vx, w * vy, w * vz};
         const R cs = sqrt(cs2);
         const R denom = R(1.0) - v2 * cs2;
         const R rad = vmax((R(1.0) - v2) * (R(1.0) - vd * vd - cs2 * (v2 - vd * vd)), R(0.0));
@@ -305,8 +392,9 @@ BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2) {
         const R b = cs * sqrt(rad) / denom;
         s.lm = a - b;
         s.lp = a + b;
+        // energy flux (E + p) v_d = w v_d; the reference's order for the plain form
+        s.f = V4<R>{PERT ? w * vd : (s.u.x + p) * vd, s.u.y * vd, s.u.z * vd, s.u.w * vd};
     }
-    s.f = V4<R>{(s.u.x + p) * vd, s.u.y * vd, s.u.z * vd, s.u.w * vd};
     if constexpr (AXIS == 0) s.f.y = s.f.y + p;
     if constexpr (AXIS == 1) s.f.z = s.f.z + p;
     if constexpr (AXIS == 2) s.f.w = s.f.w + p;
@@ -315,10 +403,10 @@ BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2) {
 
 // hll_flux(q_l, q_r, axis).  The phi arguments of the reference's hll_flux
 // reach only the bag EOS functions, which ignore them, so they are dropped.
-template <int AXIS, typename R, bool FAST>
-BUBBLE_DEV V4<R> hll_flux(const V4<R> &ql, const V4<R> &qr, R zmax2) {
-    const FaceSide<R> L = face_side<AXIS, R, FAST>(ql, zmax2);
-    const FaceSide<R> Rt = face_side<AXIS, R, FAST>(qr, zmax2);
+template <int AXIS, typename R, bool FAST, bool PERT = false>
+BUBBLE_DEV V4<R> hll_flux(const V4<R> &ql, const V4<R> &qr, R zmax2, R p_bg = R(0)) {
+    const FaceSide<R> L = face_side<AXIS, R, FAST, PERT>(ql, zmax2, p_bg);
+    const FaceSide<R> Rt = face_side<AXIS, R, FAST, PERT>(qr, zmax2, p_bg);
     const R s_min = vmin(vmin(L.lm, Rt.lm), R(0.0));
     const R s_max = vmax(vmax(L.lp, Rt.lp), R(0.0));
     const R den = vmax(s_max - s_min, R(1e-12));

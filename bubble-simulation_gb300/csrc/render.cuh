@@ -35,7 +35,7 @@ struct VisConsts {
 
 BUBBLE_DEV unsigned short half_bits(float x) { return __half_as_ushort(__float2half_rn(x)); }
 
-template <typename R, bool MIXED>
+template <typename R, int MIXED>
 __global__ void __launch_bounds__(256) vis_kernel(const V2<R> *__restrict__ field, const V4<R> *__restrict__ fluid,
                                                   LatticeParams<R> P, VisConsts<R> C, cudaSurfaceObject_t surf) {
     const uint64_t n = (uint64_t)P.nx * P.ny * P.nz;
@@ -48,12 +48,14 @@ __global__ void __launch_bounds__(256) vis_kernel(const V2<R> *__restrict__ fiel
         const R phi = field[i].x;
         const V4<R> u = fluid[i];
         const V4<R> q = recover<R, false, MIXED>(u, P);
-        const R p = q.w;
-        const R e_lab = vmax(u.x, P.e_floor);
+        // the full p and max(E, e_floor); the perturbation form adds its backgrounds
+        const R p = MIXED == kPert ? P.p_bg + q.w : q.w;
+        const R e_lab = MIXED == kPert ? P.e_bg + vmax(u.x, P.e_floor) : vmax(u.x, P.e_floor);
         const R v2 = q.x * q.x + q.y * q.y + q.z * q.z;
         const R speed = sqrt(v2);
         // eos_temperature (shaders/eos.wgsl:65-69)
-        const R temp = sqrt(sqrt(R(3.0) * vmax(p, P.p_floor) / C.a_rad));
+        const R pt = MIXED == kPert ? P.p_bg + vmax(q.w, P.p_floor) : vmax(p, P.p_floor);
+        const R temp = sqrt(sqrt(R(3.0) * pt / C.a_rad));
         const R kinetic = (e_lab + p) * v2;
         ushort4 t;
         t.x = half_bits((float)(phi / P.phi_b));

@@ -384,7 +384,7 @@ int Simulation::visualise(std::string &err) {
                             (double)h.a_rad, (double)h.t_ref, vis_surf_, stream_);
     } else {
         e = launch::vis_f32((const V2<float> *)field_[cur_], (const V4<float> *)fluid_[cur_], params_f32(), h.a_rad,
-                            h.t_ref, spec_.precision == BUBBLE_PRECISION_MIXED, vis_surf_, stream_);
+                            h.t_ref, arith_mode(), vis_surf_, stream_);
     }
     VIS_CUDA(e, "vis kernel");
     ++launches_;

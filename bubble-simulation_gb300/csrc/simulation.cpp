@@ -76,7 +76,7 @@ int Simulation::create(const bubble_spec &spec, std::unique_ptr<Simulation> &out
         err = gmsg;
         return BUBBLE_ERR_INVALID;
     }
-    if (spec.precision < BUBBLE_PRECISION_SINGLE || spec.precision > BUBBLE_PRECISION_DOUBLE) {
+    if (spec.precision < BUBBLE_PRECISION_SINGLE || spec.precision > BUBBLE_PRECISION_PERTURBATION) {
         err = "unknown precision";
         return BUBBLE_ERR_INVALID;
     }
@@ -204,7 +204,23 @@ LatticeParams<float> Simulation::params_f32() const {
     p.e_floor = h.e_floor;
     p.z_max = h.z_max;
     p.e_ref = h.e_ref;
+    if (spec_.precision == BUBBLE_PRECISION_PERTURBATION) {
+        // the stored energy is E - e_bg and the primitive pressure p - p_bg;
+        // the floors move with them
+        p.e_bg = h.e_ref;
+        p.p_bg = h.e_ref / 3.0f;
+        p.e_floor = h.e_floor - p.e_bg;
+        p.p_floor = h.p_floor - p.p_bg;
+    }
     return p;
+}
+
+int Simulation::arith_mode() const {
+    switch (spec_.precision) {
+        case BUBBLE_PRECISION_MIXED: return 1;
+        case BUBBLE_PRECISION_PERTURBATION: return 2;
+        default: return 0;
+    }
 }
 
 LatticeParams<double> Simulation::params_f64() const {
@@ -235,7 +251,7 @@ int Simulation::launch_init(std::string &err) {
                              (double)params_f32().e_ref, stream_);
     else
         e = launch::init_f32((V2<float> *)field_[cur_], (V4<float> *)fluid_[cur_], n_cells_,
-                             params_f32().e_ref, stream_);
+                             params_f32().e_ref - params_f32().e_bg, stream_);
     ++launches_;
     BUBBLE_CUDA(e, "init kernel");
     return BUBBLE_OK;
@@ -287,9 +303,10 @@ int Simulation::resize(const uint32_t grid[3], std::string &err) {
 
 int Simulation::set_tile(TileShape t, std::string &err) {
     const bool strict = !is_f64() && spec_.math == BUBBLE_MATH_STRICT;
+    const bool pert = spec_.precision == BUBBLE_PRECISION_PERTURBATION;
     // the synchronous-staging and strict kernels are built for fewer shapes
     // than the default one; their launches check the shape themselves
-    if (t.tx != 32 || !launch::v2_shape_supported(is_f64(), t.ty) || (strict && t.ty != 8) || t.lz < 1) {
+    if (t.tx != 32 || !launch::v2_shape_supported(is_f64(), t.ty) || ((strict || pert) && t.ty != 8) || t.lz < 1) {
         err = "unsupported tile shape";
         return BUBBLE_ERR_INVALID;
     }
@@ -359,6 +376,11 @@ int Simulation::stage_launch(int stage, uint32_t in_slot, uint32_t out_slot, std
     const uint64_t n = n_cells_;
     cudaError_t e = cudaSuccess;
     const bool mixed = spec_.precision == BUBBLE_PRECISION_MIXED;
+    const int mode = arith_mode();
+    if (mode == 2 && path_ != KernelPath::Fused) {
+        err = "the perturbation form runs on the default (fused, asynchronous staging) kernel path only";
+        return BUBBLE_ERR_INVALID;
+    }
     if (is_f64()) {
         StageArgs<double> A;
         A.field_n = (const V2<double> *)field_[cur_];
@@ -408,9 +430,9 @@ int Simulation::stage_launch(int stage, uint32_t in_slot, uint32_t out_slot, std
         } else {
             const int tma = tma_ok_ ? 1 : 0;
             if (spec_.math == BUBBLE_MATH_STRICT)
-                e = launch::stage_v2_f32_strict(A, P, tile_, mixed, maps_[in_slot], tma, d_status_, stream_);
+                e = launch::stage_v2_f32_strict(A, P, tile_, mode, maps_[in_slot], tma, d_status_, stream_);
             else
-                e = launch::stage_v2_f32_fast(A, P, tile_, mixed, maps_[in_slot], tma, d_status_, stream_);
+                e = launch::stage_v2_f32_fast(A, P, tile_, mode, maps_[in_slot], tma, d_status_, stream_);
             launches_ += 1;
         }
     }
@@ -470,7 +492,7 @@ int Simulation::diagnostics(bubble_diag *out, std::string &err) {
                              params_f64(), partials_, ticket_, d_result_, stream_);
     } else {
         e = launch::diag_f32((const V2<float> *)field_[cur_], (const V4<float> *)fluid_[cur_],
-                             params_f32(), spec_.precision == BUBBLE_PRECISION_MIXED, partials_,
+                             params_f32(), arith_mode(), partials_,
                              ticket_, d_result_, stream_);
     }
     ++launches_;
@@ -482,7 +504,13 @@ int Simulation::diagnostics(bubble_diag *out, std::string &err) {
         const int rc = check_status(err);
         if (rc != BUBBLE_OK) return rc;
     }
-    const DiagResult &r = *h_result_;
+    DiagResult r = *h_result_;
+    if (spec_.precision == BUBBLE_PRECISION_PERTURBATION) {
+        // the kernel summed E - e_bg: add the background in FP64
+        const double bg = (double)params_f32().e_bg * (double)n_cells_;
+        r.sums[0] += bg;
+        r.sums[3] += bg;
+    }
     // Diagnostics (src/gpu/sim.rs:991-1010): sums / cells.
     const float inv_n = 1.0f / (float)n_cells_;
     bubble_diag d{};

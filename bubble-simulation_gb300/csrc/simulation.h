@@ -101,6 +101,8 @@ class Simulation {
     LatticeParams<float> params_f32() const;
     LatticeParams<double> params_f64() const;
     bool is_f64() const { return spec_.precision == BUBBLE_PRECISION_DOUBLE; }
+    // 0 plain, 1 mixed, 2 perturbation form (the kernels' MODE parameter)
+    int arith_mode() const;
     size_t elem_field() const { return is_f64() ? 16 : 8; }
     size_t elem_fluid() const { return is_f64() ? 32 : 16; }
 

@@ -160,7 +160,7 @@ BUBBLE_DEV void cross_item(int k, int &i, int &j) {
 // when a bounded wait expired (bit 0 of *status is set); the CTA must then
 // stop.  Usable repeatedly by one CTA: it starts with a barrier and leaves
 // no copy in flight.
-template <typename R, bool FAST, bool MIXED, int TY>
+template <typename R, bool FAST, int MIXED, int TY>
 BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const LatticeParams<R> &P, int lz,
                         const StageMaps *maps, int tma_ok, int *status, int tile_xy, int chunk) {
     using L = V2Layout<R, TY>;
@@ -274,7 +274,7 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
         z_states(z0 - 1, n, lo_m, hi_m);
         z_states(z0, n, lo_0, hi_0);
         zhi[((z0 + 8) & 1) * NC + n] = hi_0;
-        fzs[((z0 - 1 + 8) & 1) * NC + n] = hll_flux<2, R, FAST>(hi_m, lo_0, zmax2);
+        fzs[((z0 - 1 + 8) & 1) * NC + n] = hll_flux<2, R, FAST, MIXED == kPert>(hi_m, lo_0, zmax2, P.p_bg);
     }
     __syncthreads();
     stage_plane_sync(z0 + 2);
@@ -428,18 +428,18 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
             } else {
                 const int kk = k - L::Y_A;
                 if (kk < L::Y_Z) {
-                    fzs[((z + 8) & 1) * NC + kk] = hll_flux<2, R, FAST>(zhi[((z + 8) & 1) * NC + kk], zlo[kk], zmax2);
+                    fzs[((z + 8) & 1) * NC + kk] = hll_flux<2, R, FAST, MIXED == kPert>(zhi[((z + 8) & 1) * NC + kk], zlo[kk], zmax2, P.p_bg);
                 } else if (kk < L::Y_Z + L::Y_Y) {
                     const int q = kk - L::Y_Z;
                     const int f = q / TX;  // face between rows f-1 and f
                     const int i = q - f * TX;
-                    fys[f * TX + i] = hll_flux<1, R, FAST>(yhi[f * TX + i], ylo[(f + 1) * TX + i], zmax2);
+                    fys[f * TX + i] = hll_flux<1, R, FAST, MIXED == kPert>(yhi[f * TX + i], ylo[(f + 1) * TX + i], zmax2, P.p_bg);
                 } else {
                     const int q = kk - L::Y_Z - L::Y_Y;
                     const int j = q / (TX + 1);
                     const int f = q - j * (TX + 1);  // face between columns f-1 and f
                     fxs[j * (TX + 1) + f] =
-                        hll_flux<0, R, FAST>(xhi[j * (TX + 2) + f], xlo[j * (TX + 2) + f + 1], zmax2);
+                        hll_flux<0, R, FAST, MIXED == kPert>(xhi[j * (TX + 2) + f], xlo[j * (TX + 2) + f + 1], zmax2, P.p_bg);
                 }
             }
         }
@@ -448,7 +448,7 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
     return true;
 }
 
-template <typename R, bool FAST, bool MIXED, int TY>
+template <typename R, bool FAST, int MIXED, int TY>
 __global__ void __launch_bounds__(V2Layout<R, TY>::NT, V2Layout<R, TY>::MIN_BLOCKS)
     stage_v2_kernel(StageArgs<R> A, LatticeParams<R> P, int lz, const __grid_constant__ StageMaps maps,
                     int tma_ok, int *status) {

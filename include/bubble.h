@@ -121,6 +121,11 @@ int bubble_make_schedule(int32_t mode, uint64_t count, float radius,
 #define BUBBLE_PRECISION_SINGLE 0 /* FP32 state, FP64 reductions           */
 #define BUBBLE_PRECISION_MIXED 1  /* SINGLE + FP64 con2prim where gamma > 3 */
 #define BUBBLE_PRECISION_DOUBLE 2 /* FP64 state and arithmetic throughout   */
+/* MIXED with the fluid energy stored as E - e_ref and the pressure carried
+ * as p - e_ref/3, so the weak-transition perturbation keeps its FP32 digits
+ * (docs/PRECISION.md:117-124 of the reference, "evolve perturbations").
+ * copy_state/load_state move the stored values: fluid.x is E - e_ref. */
+#define BUBBLE_PRECISION_PERTURBATION 3
 /* Arithmetic mode of the FP32 kernels. */
 #define BUBBLE_MATH_FAST 0   /* FMA contraction, shared reciprocals        */
 #define BUBBLE_MATH_STRICT 1 /* no contraction, IEEE div/sqrt, the WGSL

@@ -164,8 +164,36 @@ inline vec4<R> eos_regularise(const SimParams<R> &P, vec4<R> u) {
     }
     return {e_lab, zx, zy, zz};
 }
+// Perturbation form (PERT): u.x holds E - e_bg and the primitive's w
+// p - p_bg, with e_bg = e_ref and p_bg = e_ref / 3, and P carries the floors
+// shifted by the backgrounds.  p = (E^2 - Z^2) / (E + s) equals
+// E/3 - Z^2 / (s + 2E) (s = sqrt(4E^2 - 3Z^2)), so
+// p - p_bg = (E - e_bg)/3 - Z^2 / (s + 2E): the backgrounds cancel exactly.
 template <typename R>
+inline vec4<R> eos_prim_from_cons_pert(const SimParams<R> &P, vec4<R> u) {
+    const R e_bg = P.e_ref, p_bg = P.e_ref / R(3.0);
+    const R de = wmax(u.x, P.e_floor);
+    const R e_lab = e_bg + de;
+    R zx = u.y, zy = u.z, zz = u.w;
+    const R zlen = length3(zx, zy, zz);
+    const R zcap = P.z_max * e_lab;
+    if (zlen > zcap) {
+        const R sc = zcap / wmax(zlen, R(1e-30));
+        zx = zx * sc;
+        zy = zy * sc;
+        zz = zz * sc;
+    }
+    const R z2 = zx * zx + zy * zy + zz * zz;
+    const R sq = std::sqrt(wmax(R(4.0) * e_lab * e_lab - R(3.0) * z2, R(0.0)));
+    R dp = de / R(3.0) - z2 / (sq + R(2.0) * e_lab);
+    dp = wmax(dp, P.p_floor);
+    const R d = wmax(e_lab + p_bg + dp, R(1e-30));
+    return {zx / d, zy / d, zz / d, dp};
+}
+
+template <typename R, bool PERT = false>
 inline vec4<R> eos_prim_from_cons(const SimParams<R> &P, vec4<R> u_raw, R phi) {
+    if (PERT) return eos_prim_from_cons_pert(P, u_raw);
     const vec4<R> u = eos_regularise(P, u_raw);
     const R e_lab = u.x;
     const R p = eos_pressure_from_conserved(P, e_lab, u.y * u.y + u.z * u.z + u.w * u.w, phi);
@@ -173,22 +201,29 @@ inline vec4<R> eos_prim_from_cons(const SimParams<R> &P, vec4<R> u_raw, R phi) {
     const R d = wmax(s, R(1e-30));
     return {u.y / d, u.z / d, u.w / d, p};
 }
-template <typename R>
-inline vec4<R> eos_cons_from_prim(const SimParams<R> &P, vec4<R> q, R phi) {
+// PERT: the energy component is E - e_bg = w W^2 v^2 + 3 (p - p_bg); `w_out`
+// returns w W^2 for the energy flux w W^2 v_d.
+template <typename R, bool PERT = false>
+inline vec4<R> eos_cons_from_prim(const SimParams<R> &P, vec4<R> q, R phi, R *w_out = nullptr) {
     const R p = q.w;
     const R v2 = wmin(q.x * q.x + q.y * q.y + q.z * q.z, P.z_max * P.z_max);
-    const R w_gam2 = eos_enthalpy_from_pressure(p, phi) / (R(1.0) - v2);
+    const R pf = PERT ? P.e_ref / R(3.0) + p : p;
+    const R w_gam2 = eos_enthalpy_from_pressure(pf, phi) / (R(1.0) - v2);
+    if (w_out) *w_out = w_gam2;
+    if (PERT) return {w_gam2 * v2 + R(3.0) * p, w_gam2 * q.x, w_gam2 * q.y, w_gam2 * q.z};
     return {w_gam2 - p, w_gam2 * q.x, w_gam2 * q.y, w_gam2 * q.z};
 }
 template <typename R>
 inline R axis_comp(vec4<R> q, int axis) {
     return axis == 0 ? q.x : (axis == 1 ? q.y : q.z);
 }
-template <typename R>
-inline vec4<R> eos_flux(vec4<R> q, vec4<R> u, int axis) {
+// PERT: the energy flux is w W^2 v_d (passed as w), the momentum flux carries
+// p - p_bg (the constant p_bg cancels in every flux difference).
+template <typename R, bool PERT = false>
+inline vec4<R> eos_flux(vec4<R> q, vec4<R> u, int axis, R w = R(0)) {
     const R p = q.w;
     const R vd = axis_comp(q, axis);
-    vec4<R> f{(u.x + p) * vd, u.y * vd, u.z * vd, u.w * vd};
+    vec4<R> f{PERT ? w * vd : (u.x + p) * vd, u.y * vd, u.z * vd, u.w * vd};
     if (axis == 0) f.y = f.y + p;
     if (axis == 1) f.z = f.z + p;
     if (axis == 2) f.w = f.w + p;
@@ -226,12 +261,13 @@ inline vec4<R> sanitise(const SimParams<R> &P, vec4<R> q) {
     return {vx, vy, vz, p};
 }
 
-template <typename R>
+template <typename R, bool PERT = false>
 inline vec4<R> hll_flux(const SimParams<R> &P, vec4<R> q_l, R phi_l, vec4<R> q_r, R phi_r, int axis) {
-    const vec4<R> u_l = eos_cons_from_prim(P, q_l, phi_l);
-    const vec4<R> u_r = eos_cons_from_prim(P, q_r, phi_r);
-    const vec4<R> f_l = eos_flux(q_l, u_l, axis);
-    const vec4<R> f_r = eos_flux(q_r, u_r, axis);
+    R w_l, w_r;
+    const vec4<R> u_l = eos_cons_from_prim<R, PERT>(P, q_l, phi_l, &w_l);
+    const vec4<R> u_r = eos_cons_from_prim<R, PERT>(P, q_r, phi_r, &w_r);
+    const vec4<R> f_l = eos_flux<R, PERT>(q_l, u_l, axis, w_l);
+    const vec4<R> f_r = eos_flux<R, PERT>(q_r, u_r, axis, w_r);
     R lml, lpl, lmr, lpr;
     eos_wave_speeds(P, q_l, phi_l, axis, lml, lpl);
     eos_wave_speeds(P, q_r, phi_r, axis, lmr, lpr);
@@ -264,7 +300,7 @@ inline vec4<R> ld4(const R *a, size_t i) {
 }
 
 // step.wgsl main for one cell.
-template <typename R>
+template <typename R, bool PERT = false>
 void step_cell(const SimParams<R> &P, const StageParams<R> &S, const R *field_n, const R *fluid_n,
                const R *field_in, const R *fluid_in, const R *prim, R *field_out, R *fluid_out,
                int cx, int cy, int cz) {
@@ -292,9 +328,9 @@ void step_cell(const SimParams<R> &P, const StageParams<R> &S, const R *field_n,
         const vec4<R> slope_m1 = limit_slope4(sub(qm1, qm2), sub(q0, qm1));
         const vec4<R> slope_0 = limit_slope4(sub(q0, qm1), sub(qp1, q0));
         const vec4<R> slope_p1 = limit_slope4(sub(qp1, q0), sub(qp2, qp1));
-        const vec4<R> f_minus = hll_flux(P, sanitise(P, add(qm1, scale(R(0.5), slope_m1))), phi_m,
+        const vec4<R> f_minus = hll_flux<R, PERT>(P, sanitise(P, add(qm1, scale(R(0.5), slope_m1))), phi_m,
                                          sanitise(P, sub(q0, scale(R(0.5), slope_0))), phi0, axis);
-        const vec4<R> f_plus = hll_flux(P, sanitise(P, add(q0, scale(R(0.5), slope_0))), phi0,
+        const vec4<R> f_plus = hll_flux<R, PERT>(P, sanitise(P, add(q0, scale(R(0.5), slope_0))), phi0,
                                         sanitise(P, sub(qp1, scale(R(0.5), slope_p1))), phi_p, axis);
         flux_div = add(flux_div, scale(P.inv_dx, sub(f_plus, f_minus)));
     }
@@ -403,7 +439,7 @@ void nucleate_all(const SimParams<R> &P, const float *bubbles, uint32_t count, R
     }
 }
 
-template <typename R>
+template <typename R, bool PERT = false>
 void step_all(const SimParams<R> &P, const StageParams<R> &S, const R *field_n, const R *fluid_n,
               const R *field_in, const R *fluid_in, const R *prim, R *field_out, R *fluid_out) {
     const int nx = (int)P.nx, ny = (int)P.ny, nz = (int)P.nz;
@@ -411,15 +447,15 @@ void step_all(const SimParams<R> &P, const StageParams<R> &S, const R *field_n, 
     for (int z = 0; z < nz; ++z)
         for (int y = 0; y < ny; ++y)
             for (int x = 0; x < nx; ++x)
-                step_cell(P, S, field_n, fluid_n, field_in, fluid_in, prim, field_out, fluid_out, x, y, z);
+                step_cell<R, PERT>(P, S, field_n, fluid_n, field_in, fluid_in, prim, field_out, fluid_out, x, y, z);
 }
 
-template <typename R>
+template <typename R, bool PERT = false>
 void primitives_all(const SimParams<R> &P, const R *field, const R *fluid, R *prim) {
     const size_t n = (size_t)P.nx * P.ny * P.nz;
 #pragma omp parallel for schedule(static)
     for (long long i = 0; i < (long long)n; ++i) {
-        const vec4<R> q = eos_prim_from_cons(P, ld4(fluid, (size_t)i), field[2 * i]);
+        const vec4<R> q = eos_prim_from_cons<R, PERT>(P, ld4(fluid, (size_t)i), field[2 * i]);
         prim[4 * i] = q.x;
         prim[4 * i + 1] = q.y;
         prim[4 * i + 2] = q.z;
@@ -442,7 +478,9 @@ void init_all(const SimParams<R> &P, R *field, R *fluid) {
 
 // cell_contribution (reduce.wgsl:56-79) per cell in R; sums in FP64, one
 // partial per z-plane, planes folded in order.
-template <typename R>
+// PERT: e_total and e_lab miss e_bg per cell (the caller adds N e_bg in FP64);
+// the kinetic term adds e_bg + p_bg back.
+template <typename R, bool PERT = false>
 void reduce_all(const SimParams<R> &P, const R *field, const R *fluid, const R *prim, double sums[4],
                 R *max_v) {
     const int nx = (int)P.nx, ny = (int)P.ny, nz = (int)P.nz;
@@ -471,7 +509,7 @@ void reduce_all(const SimParams<R> &P, const R *field, const R *fluid, const R *
                 const R v2 = q.x * q.x + q.y * q.y + q.z * q.z;
                 const R e_total = R(0.5) * pi * pi + R(0.5) * grad2 + potential(P, phi) + e_lab;
                 const R broken = phi > R(0.5) * P.phi_b ? R(1.0) : R(0.0);
-                const R kinetic = (e_lab + q.w) * v2;
+                const R kinetic = PERT ? ((e_lab + q.w) + (P.e_ref + P.e_ref / R(3.0))) * v2 : (e_lab + q.w) * v2;
                 a0 += (double)e_total;
                 a1 += (double)broken;
                 a2 += (double)kinetic;
@@ -534,17 +572,20 @@ inline float f16_to_f32(uint16_t h) {
 
 // vis main (shaders/vis.wgsl:30-55) over a primitives buffer from
 // primitives_all; out = nx*ny*nz half4 texels.
-template <typename R>
+template <typename R, bool PERT = false>
 void vis_all(const SimParams<R> &P, const R *field, const R *fluid, const R *prim, uint16_t *out) {
     const int64_t n = (int64_t)P.nx * P.ny * P.nz;
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) {
         const R phi = field[2 * i];
-        const R vx = prim[4 * i], vy = prim[4 * i + 1], vz = prim[4 * i + 2], p = prim[4 * i + 3];
-        const R e_lab = wmax(fluid[4 * i], P.e_floor);
+        const R vx = prim[4 * i], vy = prim[4 * i + 1], vz = prim[4 * i + 2], q_w = prim[4 * i + 3];
+        const R p_bg = P.e_ref / R(3.0);
+        const R p = PERT ? p_bg + q_w : q_w;
+        const R e_lab = PERT ? P.e_ref + wmax(fluid[4 * i], P.e_floor) : wmax(fluid[4 * i], P.e_floor);
         const R vv = vx * vx + vy * vy + vz * vz;
         const R speed = std::sqrt(vv);
-        const R x = R(3.0) * wmax(p, P.p_floor) / P.a_rad;  // eos_temperature (shaders/eos.wgsl:65-69)
+        const R pt = PERT ? p_bg + wmax(q_w, P.p_floor) : wmax(p, P.p_floor);
+        const R x = R(3.0) * pt / P.a_rad;  // eos_temperature (shaders/eos.wgsl:65-69)
         const R temp = std::sqrt(std::sqrt(x));
         const R kinetic = (e_lab + p) * vv;
         out[4 * i + 0] = f32_to_f16((float)(phi / P.phi_b));
@@ -855,6 +896,36 @@ void oracle_set_threads(int n) {
 
 ORACLE_API(float, f32)
 ORACLE_API(double, f64)
+
+// The perturbation form in FP32: the same kernels over E - e_ref, with the
+// floors shifted by the backgrounds as the library's host shifts them.
+static SimParams<float> pert_params(const SimParams<float> &P) {
+    SimParams<float> Q = P;
+    Q.e_floor = P.e_floor - P.e_ref;
+    Q.p_floor = P.p_floor - P.e_ref / 3.0f;
+    return Q;
+}
+void oracle_init_pert_f32(const SimParams<float> *P, float *field, float *fluid) {
+    init_all(*P, field, fluid);
+    const size_t n = (size_t)P->nx * P->ny * P->nz;
+    for (size_t i = 0; i < n; ++i) fluid[4 * i] = 0.0f;
+}
+void oracle_primitives_pert_f32(const SimParams<float> *P, const float *field, const float *fluid, float *prim) {
+    primitives_all<float, true>(pert_params(*P), field, fluid, prim);
+}
+void oracle_step_pert_f32(const SimParams<float> *P, const StageParams<float> *S, const float *field_n,
+                          const float *fluid_n, const float *field_in, const float *fluid_in, const float *prim,
+                          float *field_out, float *fluid_out) {
+    step_all<float, true>(pert_params(*P), *S, field_n, fluid_n, field_in, fluid_in, prim, field_out, fluid_out);
+}
+void oracle_reduce_pert_f32(const SimParams<float> *P, const float *field, const float *fluid, const float *prim,
+                            double *sums, float *max_v) {
+    reduce_all<float, true>(pert_params(*P), field, fluid, prim, sums, max_v);
+}
+void oracle_vis_pert_f32(const SimParams<float> *P, const float *field, const float *fluid, const float *prim,
+                         uint16_t *out) {
+    vis_all<float, true>(pert_params(*P), field, fluid, prim, out);
+}
 
 void oracle_vis_f32(const SimParams<float> *P, const float *field, const float *fluid, const float *prim,
                     uint16_t *out) {

@@ -63,19 +63,19 @@ def lib() -> ctypes.CDLL:
             build()
         L = ctypes.CDLL(str(LIB_PATH))
         P = ctypes.c_void_p
-        for sfx in ("f32", "f64"):
+        for sfx in ("f32", "f64", "pert_f32"):
             getattr(L, f"oracle_init_{sfx}").argtypes = [P, P, P]
-            getattr(L, f"oracle_nucleate_{sfx}").argtypes = [P, P, ctypes.c_uint32, P]
             getattr(L, f"oracle_primitives_{sfx}").argtypes = [P, P, P, P]
             getattr(L, f"oracle_step_{sfx}").argtypes = [P] * 9
             getattr(L, f"oracle_reduce_{sfx}").argtypes = [P, P, P, P, P, P]
+            getattr(L, f"oracle_vis_{sfx}").argtypes = [P] * 5
+        for sfx in ("f32", "f64"):
+            getattr(L, f"oracle_nucleate_{sfx}").argtypes = [P, P, ctypes.c_uint32, P]
         L.oracle_tanh_f64.argtypes = [ctypes.c_double]
         L.oracle_tanh_f64.restype = ctypes.c_double
         L.oracle_tanh_f32.argtypes = [ctypes.c_float]
         L.oracle_tanh_f32.restype = ctypes.c_float
         L.oracle_set_threads.argtypes = [ctypes.c_int]
-        L.oracle_vis_f32.argtypes = [P] * 5
-        L.oracle_vis_f64.argtypes = [P] * 5
         L.oracle_render.argtypes = [P, P] + [ctypes.c_int] * 6 + [P]
         L.oracle_f32_to_f16.argtypes = [ctypes.c_float]
         L.oracle_f32_to_f16.restype = ctypes.c_uint16
@@ -322,14 +322,19 @@ class OracleSim:
     """CPU restatement of `Simulation` (src/gpu/sim.rs:180-1026)."""
 
     def __init__(self, grid, model: dict | None = None, schedule=None, precision: str = "f32"):
+        """precision: "f32", "f64", or "pert" (FP32 perturbation form: the
+        fluid energy stored as E - e_ref, include/bubble.h
+        BUBBLE_PRECISION_PERTURBATION without its FP64 fallback)."""
         self.model = dict(DEFAULT_MODEL, **(model or {}))
         err = validate(self.model)
         if err:
             raise ValueError(err)
         self.grid = tuple(int(g) for g in grid)
         self.n = self.grid[0] * self.grid[1] * self.grid[2]
-        self.dtype = np.float32 if precision == "f32" else np.float64
-        self.sfx = "f32" if precision == "f32" else "f64"
+        self.pert = precision == "pert"
+        self.dtype = np.float64 if precision == "f64" else np.float32
+        self.sfx = "f64" if precision == "f64" else "f32"
+        self.ksfx = "pert_f32" if self.pert else self.sfx  # kernels that differ in the perturbation form
         self.d = derived(self.model)
         self.P = _sim_params(self.dtype, self.model, self.grid)
         self.field = np.zeros((3, self.n, 2), dtype=self.dtype)
@@ -346,7 +351,7 @@ class OracleSim:
         self.next_event = 0
         if schedule is not None:
             self.schedule = list(schedule)
-        getattr(lib(), f"oracle_init_{self.sfx}")(_ptr(self.P), _ptr(self.field[0]), _ptr(self.fluid[0]))
+        getattr(lib(), f"oracle_init_{self.ksfx}")(_ptr(self.P), _ptr(self.field[0]), _ptr(self.fluid[0]))
 
     def set_state(self, field: np.ndarray, fluid: np.ndarray):
         self.field[self.cur] = field.reshape(self.n, 2)
@@ -374,9 +379,9 @@ class OracleSim:
         L = lib()
         a0, a1 = (RK3_F32 if self.dtype == np.float32 else RK3_F64)[stage]
         S = np.array([a0, a1, self.d["dt"], 0.0], dtype=self.dtype)
-        getattr(L, f"oracle_primitives_{self.sfx}")(_ptr(self.P), _ptr(self.field[in_slot]),
+        getattr(L, f"oracle_primitives_{self.ksfx}")(_ptr(self.P), _ptr(self.field[in_slot]),
                                                     _ptr(self.fluid[in_slot]), _ptr(self.prim))
-        getattr(L, f"oracle_step_{self.sfx}")(
+        getattr(L, f"oracle_step_{self.ksfx}")(
             _ptr(self.P), _ptr(S), _ptr(self.field[self.cur]), _ptr(self.fluid[self.cur]),
             _ptr(self.field[in_slot]), _ptr(self.fluid[in_slot]), _ptr(self.prim),
             _ptr(self.field[out_slot]), _ptr(self.fluid[out_slot]))
@@ -408,25 +413,28 @@ class OracleSim:
         """The vis texture of the current slot as (nz, ny, nx, 4) uint16
         (binary16 bits of phi/phi_b, |v|, T/T_ref - 1, (E+p)v^2/e_ref)."""
         L = lib()
-        getattr(L, f"oracle_primitives_{self.sfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
+        getattr(L, f"oracle_primitives_{self.ksfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
                                                     _ptr(self.fluid[self.cur]), _ptr(self.prim))
         nx, ny, nz = self.grid
         out = np.zeros((nz, ny, nx, 4), dtype=np.uint16)
-        getattr(L, f"oracle_vis_{self.sfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
+        getattr(L, f"oracle_vis_{self.ksfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
                                              _ptr(self.fluid[self.cur]), _ptr(self.prim), _ptr(out))
         return out
 
     # record_visualisation's primitives pass + reduce (src/gpu/sim.rs:918-1010)
     def diagnostics(self) -> dict:
         L = lib()
-        getattr(L, f"oracle_primitives_{self.sfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
+        getattr(L, f"oracle_primitives_{self.ksfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
                                                     _ptr(self.fluid[self.cur]), _ptr(self.prim))
         sums = np.zeros(4, dtype=np.float64)
         vmax = np.zeros(1, dtype=self.dtype)
-        getattr(L, f"oracle_reduce_{self.sfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
+        getattr(L, f"oracle_reduce_{self.ksfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
                                                 _ptr(self.fluid[self.cur]), _ptr(self.prim),
                                                 _ptr(sums), _ptr(vmax))
         n = self.n
+        if self.pert:  # the kernel summed E - e_ref: add the background in FP64
+            sums[0] += float(self.d["e_ref"]) * n
+            sums[3] += float(self.d["e_ref"]) * n
         inv_n = f32(f32(1.0) / f32(n))
         out = dict(sum_energy=sums[0], sum_broken=sums[1], sum_kinetic=sums[2],
                    sum_fluid_energy=sums[3], max_velocity=float(vmax[0]),
