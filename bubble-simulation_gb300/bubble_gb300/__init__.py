@@ -51,6 +51,14 @@ def derived(model: Model) -> dict:
     return {n: getattr(d, n) for n, _ in _lib.Derived._fields_}
 
 
+def validate_eos(spec: "SimulationSpec") -> str | None:
+    """The spec's equation-of-state selection: None if valid, else the message."""
+    L = load()
+    if L.bubble_eos_validate(ctypes.byref(spec.c())) == _lib.OK:
+        return None
+    return L.bubble_last_error().decode()
+
+
 def validate_model(model: Model) -> str | None:
     rc = load().bubble_model_validate(ctypes.byref(model.c()))
     return None if rc == _lib.OK else load().bubble_last_error().decode()
@@ -114,19 +122,22 @@ class SimulationSpec:
     bubbles: int = 12
     nucleation_duration: float = 60.0
     seed: int = 1
-    precision: str = "single"  # single | mixed | double
+    precision: str = "single"  # single | mixed | double | perturbation
     math: str = "fast"  # fast | strict
+    eos: str = "bag"  # bag | bag_dof (eos_param = (dof ratio, -)) | gamma_law (eos_param = (Gamma, e0))
+    eos_param: tuple = (1.0, 0.0)
 
     def c(self) -> _lib.Spec:
         return _lib.Spec(self.model.c(), (ctypes.c_uint32 * 3)(*self.grid), _lib.NUCLEATION[self.nucleation],
                          self.bubbles, self.nucleation_duration, self.seed, _lib.PRECISION[self.precision],
-                         _lib.MATH[self.math])
+                         _lib.MATH[self.math], _lib.EOS[self.eos], (ctypes.c_float * 2)(*self.eos_param))
 
     @classmethod
     def from_c(cls, c: _lib.Spec) -> "SimulationSpec":
         inv = lambda d, v: next(k for k, x in d.items() if x == v)  # noqa: E731
         return cls(Model.from_c(c.model), tuple(c.grid), inv(_lib.NUCLEATION, c.nucleation), c.bubbles,
-                   c.nucleation_duration, c.seed, inv(_lib.PRECISION, c.precision), inv(_lib.MATH, c.math))
+                   c.nucleation_duration, c.seed, inv(_lib.PRECISION, c.precision), inv(_lib.MATH, c.math),
+                   inv(_lib.EOS, c.eos), tuple(c.eos_param))
 
 
 @dataclass

@@ -27,6 +27,7 @@ SEED_CELLS = 1
 NUCLEATION = {"simultaneous": 0, "exponential": 1, "centre": 2, "uniform": 3}
 PRECISION = {"single": 0, "mixed": 1, "double": 2, "perturbation": 3}
 MATH = {"fast": 0, "strict": 1}
+EOS = {"bag": 0, "bag_dof": 1, "gamma_law": 2}
 PATH_FUSED = 0
 PATH_REFERENCE = 1
 PATH_FUSED_SYNC = 2
@@ -57,7 +58,8 @@ class Event(ctypes.Structure):
 class Spec(ctypes.Structure):
     _fields_ = [("model", Model), ("grid", ctypes.c_uint32 * 3), ("nucleation", ctypes.c_int32),
                 ("bubbles", ctypes.c_uint64), ("nucleation_duration", ctypes.c_float),
-                ("seed", ctypes.c_uint64), ("precision", ctypes.c_int32), ("math", ctypes.c_int32)]
+                ("seed", ctypes.c_uint64), ("precision", ctypes.c_int32), ("math", ctypes.c_int32),
+                ("eos", ctypes.c_int32), ("eos_param", ctypes.c_float * 2)]
 
 
 class Diag(ctypes.Structure):
@@ -141,6 +143,7 @@ SIGNATURES = [
     ("bubble_model_default", None, [ctypes.POINTER(Model)]),
     ("bubble_model_validate", ctypes.c_int, [ctypes.POINTER(Model)]),
     ("bubble_model_derived", ctypes.c_int, [ctypes.POINTER(Model), ctypes.POINTER(Derived)]),
+    ("bubble_eos_validate", ctypes.c_int, [ctypes.POINTER(Spec)]),
     ("bubble_make_schedule", ctypes.c_int, [ctypes.c_int32, ctypes.c_uint64, ctypes.c_float, _U32P,
                                             ctypes.c_float, ctypes.c_uint64, ctypes.POINTER(Event),
                                             ctypes.c_uint64, _U64P]),

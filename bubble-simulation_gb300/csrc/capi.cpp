@@ -100,6 +100,16 @@ void bubble_spec_default(bubble_spec *out) {
     out->seed = 1;
     out->precision = BUBBLE_PRECISION_SINGLE;
     out->math = BUBBLE_MATH_FAST;
+    out->eos = BUBBLE_EOS_BAG;
+    out->eos_param[0] = 1.0f;
+    out->eos_param[1] = 0.0f;
+}
+
+int bubble_eos_validate(const bubble_spec *spec) {
+    NEED(spec);
+    const std::string msg = bubble::validate_eos(*spec);
+    if (!msg.empty()) return fail(BUBBLE_ERR_INVALID, msg);
+    return BUBBLE_OK;
 }
 
 int bubble_stage_slots(uint32_t cur, uint32_t out[6]) {

@@ -200,6 +200,15 @@ int Simulation::restore_checkpoint(const std::string &path, std::string &err) {
         err = path + ": " + msg;
         return BUBBLE_ERR_INVALID;
     }
+    {
+        bubble_spec chk = h.spec;
+        chk.precision = spec_.precision;
+        const std::string emsg = validate_eos(chk);
+        if (!emsg.empty()) {
+            err = path + ": " + emsg;
+            return BUBBLE_ERR_INVALID;
+        }
+    }
     if (std::memcmp(h.spec.grid, grid_, sizeof(grid_)) != 0) {
         rc = resize(h.spec.grid, err);
         if (rc != BUBBLE_OK) return rc;

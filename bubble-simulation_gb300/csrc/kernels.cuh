@@ -153,14 +153,14 @@ __global__ void stage_ref_kernel(StageArgs<R> A, const V4<R> *__restrict__ prim,
         const V4<R> rp = sanitise(half_step(qp1, s_p1, R(-1)), P.p_floor, zmax2);
         V4<R> fm, fp;
         if (axis == 0) {
-            fm = hll_flux<0, R, false>(lm, rm, zmax2);
-            fp = hll_flux<0, R, false>(lp, rp, zmax2);
+            fm = hll_flux<0, R, false>(lm, rm, zmax2, P);
+            fp = hll_flux<0, R, false>(lp, rp, zmax2, P);
         } else if (axis == 1) {
-            fm = hll_flux<1, R, false>(lm, rm, zmax2);
-            fp = hll_flux<1, R, false>(lp, rp, zmax2);
+            fm = hll_flux<1, R, false>(lm, rm, zmax2, P);
+            fp = hll_flux<1, R, false>(lp, rp, zmax2, P);
         } else {
-            fm = hll_flux<2, R, false>(lm, rm, zmax2);
-            fp = hll_flux<2, R, false>(lp, rp, zmax2);
+            fm = hll_flux<2, R, false>(lm, rm, zmax2, P);
+            fp = hll_flux<2, R, false>(lp, rp, zmax2, P);
         }
         fd.x = fd.x + (fp.x - fm.x) * P.inv_dx;
         fd.y = fd.y + (fp.y - fm.y) * P.inv_dx;
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(TX *(TY + 1))
         z_states(z0 - 1, n, lo_m, hi_m);
         z_states(z0, n, lo_0, hi_0);
         zhi[((z0 + 8) & 1) * NC + n] = hi_0;
-        fzs[((z0 - 1 + 8) & 1) * NC + n] = hll_flux<2, R, FAST>(hi_m, lo_0, zmax2);
+        fzs[((z0 - 1 + 8) & 1) * NC + n] = hll_flux<2, R, FAST, MIXED>(hi_m, lo_0, zmax2, P);
     }
     // (the first loop iteration's barrier orders these writes)
 
@@ -364,18 +364,18 @@ __global__ void __launch_bounds__(TX *(TY + 1))
             for (int k = t; k < n_z + n_y + n_x; k += NT) {
                 if (k < n_z) {
                     fzs[((z + 8) & 1) * NC + k] =
-                        hll_flux<2, R, FAST>(zhi[((z + 8) & 1) * NC + k], zlo[k], zmax2);
+                        hll_flux<2, R, FAST, MIXED>(zhi[((z + 8) & 1) * NC + k], zlo[k], zmax2, P);
                 } else if (k < n_z + n_y) {
                     const int kk = k - n_z;
                     const int f = kk / TX;  // face between rows f-1 and f
                     const int i = kk - f * TX;
-                    fys[f * TX + i] = hll_flux<1, R, FAST>(yhi[f * TX + i], ylo[(f + 1) * TX + i], zmax2);
+                    fys[f * TX + i] = hll_flux<1, R, FAST, MIXED>(yhi[f * TX + i], ylo[(f + 1) * TX + i], zmax2, P);
                 } else {
                     const int kk = k - n_z - n_y;
                     const int j = kk / (TX + 1);
                     const int f = kk - j * (TX + 1);  // face between columns f-1 and f
                     fxs[j * (TX + 1) + f] =
-                        hll_flux<0, R, FAST>(xhi[j * (TX + 2) + f], xlo[j * (TX + 2) + f + 1], zmax2);
+                        hll_flux<0, R, FAST, MIXED>(xhi[j * (TX + 2) + f], xlo[j * (TX + 2) + f + 1], zmax2, P);
                 }
             }
         }

@@ -36,7 +36,8 @@ cudaError_t stage_ref_f32(const StageArgs<float> &A, const V4<float> *prim,
                           const LatticeParams<float> &P, cudaStream_t s);
 cudaError_t stage_fused_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P,
                                    TileShape shape, bool mixed, cudaStream_t s);
-// `mode`: 0 plain, 1 mixed, 2 perturbation form (physics.cuh kPlain/kMixed/kPert).
+// `mode`: 0 plain, 1 mixed, 2 perturbation form, 3 gamma-law equation of
+// state (physics.cuh kPlain/kMixed/kPert/kGamma).
 cudaError_t diag_f32(const V2<float> *field, const V4<float> *fluid,
                      const LatticeParams<float> &P, int mode, void *partials,
                      unsigned int *ticket, DiagResult *out, cudaStream_t s);
@@ -69,7 +70,8 @@ int diag_blocks_for(uint64_t cells);
 // whether they are valid; bit 0 of *status is set if a bounded wait expired.
 bool v2_shape_supported(int precision_double, int ty);
 size_t v2_smem_bytes(int precision_double, int ty);
-// `mode` as for diag_f32; the perturbation form is built for ty = 8 only.
+// `mode` as for diag_f32; the perturbation and gamma-law forms are built for
+// ty = 8 only.
 cudaError_t stage_v2_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
                                 int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
 cudaError_t stage_v2_f32_fast(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,

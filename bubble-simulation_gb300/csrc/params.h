@@ -36,6 +36,9 @@ struct LatticeParams {
     // (e_bg = e_ref) and from the pressure (p_bg = e_bg / 3); both 0, and the
     // floors unshifted, for the other forms.
     R e_bg, p_bg;
+    // Gamma-law equation of state: c_s^2 = Gamma - 1 and the offset e0 of
+    // e = p / (Gamma - 1) + e0; both 0 for the bag model.
+    R eos_c2, eos_e0;
 };
 
 // One SSP-RK3 stage: U_out = a0 U^n + a1 (U_in + dt L(U_in))

@@ -227,3 +227,30 @@ std::vector<bubble_event> make_schedule(int mode, uint64_t count, float radius,
 }
 
 }  // namespace bubble
+
+namespace bubble {
+
+std::string validate_eos(const bubble_spec &spec) {
+    switch (spec.eos) {
+        case BUBBLE_EOS_BAG:
+            return {};
+        case BUBBLE_EOS_BAG_DOF:
+            if (!(spec.eos_param[0] > 0.0f) || !std::isfinite(spec.eos_param[0]))
+                return "the degrees-of-freedom ratio must be positive and finite";
+            return {};
+        case BUBBLE_EOS_GAMMA_LAW: {
+            const float g = spec.eos_param[0], e0 = spec.eos_param[1];
+            if (!(g > 1.0f && g <= 2.0f)) return "Gamma must lie in (1, 2] (a causal sound speed)";
+            const float e_ref = derive(spec.model).e_ref;
+            if (!(e0 >= 0.0f && e0 < 0.99f * e_ref))
+                return "e0 must lie in [0, 0.99 e_ref) so the reference pressure is positive";
+            if (spec.precision != BUBBLE_PRECISION_SINGLE)
+                return "the gamma-law equation of state is built for BUBBLE_PRECISION_SINGLE";
+            return {};
+        }
+        default:
+            return "unknown equation of state";
+    }
+}
+
+}  // namespace bubble

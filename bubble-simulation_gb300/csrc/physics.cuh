@@ -241,14 +241,66 @@ BUBBLE_DEV V4<float> prim_from_cons_pert_f64(const V4<float> &u, const LatticePa
     return V4<float>{(float)(zx / d), (float)(zy / d), (float)(zz / d), (float)dp};
 }
 
-// Arithmetic forms of a lattice (the MODE parameter of the kernels):
-// plain; mixed = FP64 primitive recovery where the Lorentz factor exceeds 3;
-// perturbation = mixed, with E stored as E - e_bg.
-constexpr int kPlain = 0, kMixed = 1, kPert = 2;
+// ---------------------------------------------------------------------------
+//  Gamma-law equation of state e = p / (Gamma - 1) + e0 (docs/EOS.md:86-118)
+// ---------------------------------------------------------------------------
+// c_s^2 = dp/de = Gamma - 1 (P.eos_c2), w = e + p = p / c2 + p + e0.  With
+// s = E + p the closure leaves f(p) = p - c2 (E - Z^2 / s - e0) = 0, monotone
+// (f' = 1 - c2 Z^2 / s^2 > 0 for |Z| < E), solved by a fixed eight Newton
+// steps from the Z = 0 root c2 (E - e0), floored at p_floor after each step:
+// a fixed count, so no cell can stall its warp.  Gamma = 4/3, e0 = 0 is the
+// bag model.
+constexpr int kGammaNewtonSteps = 8;
+
+template <typename R>
+BUBBLE_DEV R gamma_enthalpy(R p, const LatticeParams<R> &P) {
+    return p / P.eos_c2 + p + P.eos_e0;
+}
+
+template <typename R, bool FAST>
+BUBBLE_DEV V4<R> prim_from_cons_gamma(const V4<R> &u, const LatticeParams<R> &P) {
+    const R e_lab = vmax(u.x, P.e_floor);
+    R zx = u.y, zy = u.z, zz = u.w;
+    const R zcap = P.z_max * e_lab;
+    const R zlen = sqrt(zx * zx + zy * zy + zz * zz);
+    if (zlen > zcap) {
+        const R sc = zcap / vmax(zlen, R(1e-30));
+        zx = zx * sc;
+        zy = zy * sc;
+        zz = zz * sc;
+    }
+    const R z2 = zx * zx + zy * zy + zz * zz;
+    const R c2 = P.eos_c2;
+    R p = vmax(c2 * (e_lab - P.eos_e0), P.p_floor);
+#pragma unroll
+    for (int it = 0; it < kGammaNewtonSteps; ++it) {
+        const R sp = e_lab + p;
+        if constexpr (FAST) {
+            const R inv = rcp_approx(sp);
+            const R r = p - c2 * (e_lab - z2 * inv - P.eos_e0);
+            const R d = R(1.0) - c2 * z2 * (inv * inv);
+            p = vmax(p - r * rcp_approx(d), P.p_floor);
+        } else {
+            const R r = p - c2 * (e_lab - z2 / sp - P.eos_e0);
+            const R d = R(1.0) - c2 * z2 / (sp * sp);
+            p = vmax(p - r / d, P.p_floor);
+        }
+    }
+    const R d = vmax(e_lab + p, R(1e-30));
+    return V4<R>{zx / d, zy / d, zz / d, p};
+}
+
+// Forms of a lattice (the FORM parameter of the kernels): the bag model in
+// plain FP32; mixed = FP64 primitive recovery where the Lorentz factor
+// exceeds 3; perturbation = mixed, with E stored as E - e_bg; gamma = the
+// gamma-law equation of state in plain arithmetic.
+constexpr int kPlain = 0, kMixed = 1, kPert = 2, kGamma = 3;
 
 template <typename R, bool FAST, int MODE>
 BUBBLE_DEV V4<R> recover(const V4<R> &u, const LatticeParams<R> &P) {
-    if constexpr (MODE == kPert) {
+    if constexpr (MODE == kGamma) {
+        return prim_from_cons_gamma<R, FAST>(u, P);
+    } else if constexpr (MODE == kPert) {
         V4<R> q = prim_from_cons_pert<R, FAST>(u, P);
         if constexpr (sizeof(R) == 4) {
             const R v2 = q.x * q.x + q.y * q.y + q.z * q.z;
@@ -352,11 +404,46 @@ struct FaceSide {
 // PERT: q.w is p - p_bg, the energy component of u is E - e_bg = w v^2 + 3 (p - p_bg)
 // (w = 4p W^2, e_bg = 3 p_bg), and the momentum flux carries p - p_bg: the
 // constant p_bg would cancel in every flux difference.
-template <int AXIS, typename R, bool FAST, bool PERT = false>
-BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2, R p_bg) {
+// GAMMA (FORM kGamma): w = p / c2 + p + e0 and the general wave speeds
+// with c_s^2 = c2; E = w W^2 - p and the fluxes as for the bag model.
+template <int AXIS, typename R, bool FAST, int FORM = kPlain>
+BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2, const LatticeParams<R> &P) {
+    constexpr bool PERT = FORM == kPert;
     FaceSide<R> s;
     const R vx = q.x, vy = q.y, vz = q.z, p = q.w;
-    const R pf = PERT ? p_bg + p : p;  // the full pressure
+    if constexpr (FORM == kGamma) {
+        const R vd = comp<AXIS>(q);
+        const R v2 = vmin(vx * vx + vy * vy + vz * vz, zmax2);
+        const R cs2 = P.eos_c2;
+        R w, den_inv;
+        if constexpr (FAST) {
+            w = gamma_enthalpy(p, P) * rcp_approx(R(1.0) - v2);
+            den_inv = rcp_approx(R(1.0) - v2 * cs2);
+        } else {
+            w = gamma_enthalpy(p, P) / (R(1.0) - v2);
+        }
+        s.u = V4<R>{w - p, w * vx, w * vy, w * vz};
+        const R cs = sqrt(cs2);
+        const R rad = vmax((R(1.0) - v2) * (R(1.0) - vd * vd - cs2 * (v2 - vd * vd)), R(0.0));
+        if constexpr (FAST) {
+            const R a = vd * (R(1.0) - cs2) * den_inv;
+            const R b = cs * sqrt_approx(rad) * den_inv;
+            s.lm = a - b;
+            s.lp = a + b;
+        } else {
+            const R denom = R(1.0) - v2 * cs2;
+            const R a = vd * (R(1.0) - cs2) / denom;
+            const R b = cs * sqrt(rad) / denom;
+            s.lm = a - b;
+            s.lp = a + b;
+        }
+        s.f = V4<R>{(s.u.x + p) * vd, s.u.y * vd, s.u.z * vd, s.u.w * vd};
+        if constexpr (AXIS == 0) s.f.y = s.f.y + p;
+        if constexpr (AXIS == 1) s.f.z = s.f.z + p;
+        if constexpr (AXIS == 2) s.f.w = s.f.w + p;
+        return s;
+    }
+    const R pf = PERT ? P.p_bg + p : p;  // the full pressure
     const R vd = comp<AXIS>(q);
     const R v2 = vmin(vx * vx + vy * vy + vz * vz, zmax2);
     const R cs2 = R(1.0) / R(3.0);  // eos_sound_speed2 (eos.wgsl:50-53)
@@ -403,10 +490,10 @@ BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2, R p_bg) {
 
 // hll_flux(q_l, q_r, axis).  The phi arguments of the reference's hll_flux
 // reach only the bag EOS functions, which ignore them, so they are dropped.
-template <int AXIS, typename R, bool FAST, bool PERT = false>
-BUBBLE_DEV V4<R> hll_flux(const V4<R> &ql, const V4<R> &qr, R zmax2, R p_bg = R(0)) {
-    const FaceSide<R> L = face_side<AXIS, R, FAST, PERT>(ql, zmax2, p_bg);
-    const FaceSide<R> Rt = face_side<AXIS, R, FAST, PERT>(qr, zmax2, p_bg);
+template <int AXIS, typename R, bool FAST, int FORM = kPlain>
+BUBBLE_DEV V4<R> hll_flux(const V4<R> &ql, const V4<R> &qr, R zmax2, const LatticeParams<R> &P) {
+    const FaceSide<R> L = face_side<AXIS, R, FAST, FORM>(ql, zmax2, P);
+    const FaceSide<R> Rt = face_side<AXIS, R, FAST, FORM>(qr, zmax2, P);
     const R s_min = vmin(vmin(L.lm, Rt.lm), R(0.0));
     const R s_max = vmax(vmax(L.lp, Rt.lp), R(0.0));
     const R den = vmax(s_max - s_min, R(1e-12));

@@ -56,6 +56,10 @@ struct SimParamsHost {
 };
 SimParamsHost sim_params(const bubble_model &m, const uint32_t grid[3]);
 
+// Equation-of-state selection of a spec: the policy exists, its parameters
+// are in range, and the arithmetic form supports it.  Empty string when valid.
+std::string validate_eos(const bubble_spec &spec);
+
 // RK3 (src/gpu/sim.rs:133-135).
 extern const float kRK3[3][2];
 

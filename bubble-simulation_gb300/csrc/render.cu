@@ -21,19 +21,20 @@ int vis_grid(uint64_t n) {
 }  // namespace
 
 cudaError_t vis_f32(const V2<float> *field, const V4<float> *fluid, const LatticeParams<float> &P, float a_rad,
-                    float t_ref, int mode, cudaSurfaceObject_t surf, cudaStream_t s) {
+                    float t_ref, float dof_ratio, int mode, cudaSurfaceObject_t surf, cudaStream_t s) {
     const uint64_t n = (uint64_t)P.nx * P.ny * P.nz;
-    const dev::VisConsts<float> C{a_rad, t_ref};
-    if (mode == dev::kPert) dev::vis_kernel<float, dev::kPert><<<vis_grid(n), 256, 0, s>>>(field, fluid, P, C, surf);
+    const dev::VisConsts<float> C{a_rad, t_ref, dof_ratio};
+    if (mode == dev::kGamma) dev::vis_kernel<float, dev::kGamma><<<vis_grid(n), 256, 0, s>>>(field, fluid, P, C, surf);
+    else if (mode == dev::kPert) dev::vis_kernel<float, dev::kPert><<<vis_grid(n), 256, 0, s>>>(field, fluid, P, C, surf);
     else if (mode == dev::kMixed) dev::vis_kernel<float, dev::kMixed><<<vis_grid(n), 256, 0, s>>>(field, fluid, P, C, surf);
     else dev::vis_kernel<float, dev::kPlain><<<vis_grid(n), 256, 0, s>>>(field, fluid, P, C, surf);
     return cudaGetLastError();
 }
 
 cudaError_t vis_f64(const V2<double> *field, const V4<double> *fluid, const LatticeParams<double> &P,
-                    double a_rad, double t_ref, cudaSurfaceObject_t surf, cudaStream_t s) {
+                    double a_rad, double t_ref, float dof_ratio, cudaSurfaceObject_t surf, cudaStream_t s) {
     const uint64_t n = (uint64_t)P.nx * P.ny * P.nz;
-    const dev::VisConsts<double> C{a_rad, t_ref};
+    const dev::VisConsts<double> C{a_rad, t_ref, (double)dof_ratio};
     dev::vis_kernel<double, dev::kPlain><<<vis_grid(n), 256, 0, s>>>(field, fluid, P, C, surf);
     return cudaGetLastError();
 }

@@ -31,6 +31,9 @@ namespace dev {
 template <typename R>
 struct VisConsts {
     R a_rad, t_ref;
+    // Phase-dependent radiation constant (docs/EOS.md:58-84):
+    // a(phi) = a_rad (1 + (r - 1) smoothstep(phi / phi_b)); r = 1 is the bag model.
+    R dof_ratio;
 };
 
 BUBBLE_DEV unsigned short half_bits(float x) { return __half_as_ushort(__float2half_rn(x)); }
@@ -55,7 +58,13 @@ __global__ void __launch_bounds__(256) vis_kernel(const V2<R> *__restrict__ fiel
         const R speed = sqrt(v2);
         // eos_temperature (shaders/eos.wgsl:65-69)
         const R pt = MIXED == kPert ? P.p_bg + vmax(q.w, P.p_floor) : vmax(p, P.p_floor);
-        const R temp = sqrt(sqrt(R(3.0) * pt / C.a_rad));
+        R a = C.a_rad;
+        if (C.dof_ratio != R(1.0)) {
+            const R h = vmin(vmax(phi / P.phi_b, R(0.0)), R(1.0));
+            const R smooth = h * h * (R(3.0) - R(2.0) * h);
+            a = C.a_rad * (R(1.0) + (C.dof_ratio - R(1.0)) * smooth);
+        }
+        const R temp = sqrt(sqrt(R(3.0) * pt / a));
         const R kinetic = (e_lab + p) * v2;
         ushort4 t;
         t.x = half_bits((float)(phi / P.phi_b));

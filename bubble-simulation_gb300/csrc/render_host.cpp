@@ -378,13 +378,14 @@ int Simulation::visualise(std::string &err) {
         VIS_CUDA(cudaCreateTextureObject(&vis_tex_, &res, &td, nullptr), "cudaCreateTextureObject");
     }
     const SimParamsHost h = sim_params(spec_.model, grid_);
+    const float dof = spec_.eos == BUBBLE_EOS_BAG_DOF ? spec_.eos_param[0] : 1.0f;
     cudaError_t e;
     if (is_f64()) {
         e = launch::vis_f64((const V2<double> *)field_[cur_], (const V4<double> *)fluid_[cur_], params_f64(),
-                            (double)h.a_rad, (double)h.t_ref, vis_surf_, stream_);
+                            (double)h.a_rad, (double)h.t_ref, dof, vis_surf_, stream_);
     } else {
         e = launch::vis_f32((const V2<float> *)field_[cur_], (const V4<float> *)fluid_[cur_], params_f32(), h.a_rad,
-                            h.t_ref, arith_mode(), vis_surf_, stream_);
+                            h.t_ref, dof, arith_mode(), vis_surf_, stream_);
     }
     VIS_CUDA(e, "vis kernel");
     ++launches_;

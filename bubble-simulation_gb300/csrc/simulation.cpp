@@ -88,6 +88,13 @@ int Simulation::create(const bubble_spec &spec, std::unique_ptr<Simulation> &out
         err = "unknown nucleation mode";
         return BUBBLE_ERR_INVALID;
     }
+    {
+        const std::string emsg = validate_eos(spec);
+        if (!emsg.empty()) {
+            err = emsg;
+            return BUBBLE_ERR_INVALID;
+        }
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
@@ -204,6 +211,10 @@ LatticeParams<float> Simulation::params_f32() const {
     p.e_floor = h.e_floor;
     p.z_max = h.z_max;
     p.e_ref = h.e_ref;
+    if (spec_.eos == BUBBLE_EOS_GAMMA_LAW) {
+        p.eos_c2 = spec_.eos_param[0] - 1.0f;
+        p.eos_e0 = spec_.eos_param[1];
+    }
     if (spec_.precision == BUBBLE_PRECISION_PERTURBATION) {
         // the stored energy is E - e_bg and the primitive pressure p - p_bg;
         // the floors move with them
@@ -216,6 +227,7 @@ LatticeParams<float> Simulation::params_f32() const {
 }
 
 int Simulation::arith_mode() const {
+    if (spec_.eos == BUBBLE_EOS_GAMMA_LAW) return 3;
     switch (spec_.precision) {
         case BUBBLE_PRECISION_MIXED: return 1;
         case BUBBLE_PRECISION_PERTURBATION: return 2;
@@ -272,6 +284,13 @@ int Simulation::set_model(const bubble_model &m, std::string &err) {
         err = msg;
         return BUBBLE_ERR_INVALID;
     }
+    bubble_spec next = spec_;
+    next.model = m;
+    const std::string emsg = validate_eos(next);  // e0 is bounded by the new e_ref
+    if (!emsg.empty()) {
+        err = emsg;
+        return BUBBLE_ERR_INVALID;
+    }
     spec_.model = m;
     return BUBBLE_OK;
 }
@@ -303,7 +322,7 @@ int Simulation::resize(const uint32_t grid[3], std::string &err) {
 
 int Simulation::set_tile(TileShape t, std::string &err) {
     const bool strict = !is_f64() && spec_.math == BUBBLE_MATH_STRICT;
-    const bool pert = spec_.precision == BUBBLE_PRECISION_PERTURBATION;
+    const bool pert = spec_.precision == BUBBLE_PRECISION_PERTURBATION || spec_.eos == BUBBLE_EOS_GAMMA_LAW;
     // the synchronous-staging and strict kernels are built for fewer shapes
     // than the default one; their launches check the shape themselves
     if (t.tx != 32 || !launch::v2_shape_supported(is_f64(), t.ty) || ((strict || pert) && t.ty != 8) || t.lz < 1) {
@@ -377,8 +396,9 @@ int Simulation::stage_launch(int stage, uint32_t in_slot, uint32_t out_slot, std
     cudaError_t e = cudaSuccess;
     const bool mixed = spec_.precision == BUBBLE_PRECISION_MIXED;
     const int mode = arith_mode();
-    if (mode == 2 && path_ != KernelPath::Fused) {
-        err = "the perturbation form runs on the default (fused, asynchronous staging) kernel path only";
+    if (mode >= 2 && path_ != KernelPath::Fused) {
+        err = "the perturbation form and the gamma-law equation of state run on the default (fused, "
+              "asynchronous staging) kernel path only";
         return BUBBLE_ERR_INVALID;
     }
     if (is_f64()) {

@@ -274,7 +274,7 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
         z_states(z0 - 1, n, lo_m, hi_m);
         z_states(z0, n, lo_0, hi_0);
         zhi[((z0 + 8) & 1) * NC + n] = hi_0;
-        fzs[((z0 - 1 + 8) & 1) * NC + n] = hll_flux<2, R, FAST, MIXED == kPert>(hi_m, lo_0, zmax2, P.p_bg);
+        fzs[((z0 - 1 + 8) & 1) * NC + n] = hll_flux<2, R, FAST, MIXED>(hi_m, lo_0, zmax2, P);
     }
     __syncthreads();
     stage_plane_sync(z0 + 2);
@@ -428,18 +428,18 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
             } else {
                 const int kk = k - L::Y_A;
                 if (kk < L::Y_Z) {
-                    fzs[((z + 8) & 1) * NC + kk] = hll_flux<2, R, FAST, MIXED == kPert>(zhi[((z + 8) & 1) * NC + kk], zlo[kk], zmax2, P.p_bg);
+                    fzs[((z + 8) & 1) * NC + kk] = hll_flux<2, R, FAST, MIXED>(zhi[((z + 8) & 1) * NC + kk], zlo[kk], zmax2, P);
                 } else if (kk < L::Y_Z + L::Y_Y) {
                     const int q = kk - L::Y_Z;
                     const int f = q / TX;  // face between rows f-1 and f
                     const int i = q - f * TX;
-                    fys[f * TX + i] = hll_flux<1, R, FAST, MIXED == kPert>(yhi[f * TX + i], ylo[(f + 1) * TX + i], zmax2, P.p_bg);
+                    fys[f * TX + i] = hll_flux<1, R, FAST, MIXED>(yhi[f * TX + i], ylo[(f + 1) * TX + i], zmax2, P);
                 } else {
                     const int q = kk - L::Y_Z - L::Y_Y;
                     const int j = q / (TX + 1);
                     const int f = q - j * (TX + 1);  // face between columns f-1 and f
                     fxs[j * (TX + 1) + f] =
-                        hll_flux<0, R, FAST, MIXED == kPert>(xhi[j * (TX + 2) + f], xlo[j * (TX + 2) + f + 1], zmax2, P.p_bg);
+                        hll_flux<0, R, FAST, MIXED>(xhi[j * (TX + 2) + f], xlo[j * (TX + 2) + f + 1], zmax2, P);
                 }
             }
         }

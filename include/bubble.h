@@ -132,6 +132,16 @@ int bubble_make_schedule(int32_t mode, uint64_t count, float radius,
                                 evaluation order: bit-identical with a
                                 plain IEEE single-precision restatement   */
 
+/* Equation of state.  The reference's swap point is the body of the ten
+ * eos_* functions (docs/EOS.md:10-23); here each equation of state is a
+ * compiled policy of the kernels, chosen per simulation. */
+#define BUBBLE_EOS_BAG 0       /* e = 3p, closed-form inversion: the reference's   */
+#define BUBBLE_EOS_BAG_DOF 1   /* bag with a(phi) = a_rad (1 + (r - 1) smoothstep(phi/phi_b)),
+                                  r = eos_param[0]: only T changes (docs/EOS.md:58-84) */
+#define BUBBLE_EOS_GAMMA_LAW 2 /* e = p/(Gamma - 1) + e0, c_s^2 = Gamma - 1, Newton
+                                  inversion (docs/EOS.md:86-118); Gamma = eos_param[0]
+                                  in (1, 2], e0 = eos_param[1] in [0, e_ref)          */
+
 typedef struct bubble_spec {
     bubble_model model;
     uint32_t grid[3];
@@ -141,10 +151,16 @@ typedef struct bubble_spec {
     uint64_t seed;             /* schedule seed                           */
     int32_t precision;         /* BUBBLE_PRECISION_*                      */
     int32_t math;              /* BUBBLE_MATH_*                           */
+    int32_t eos;               /* BUBBLE_EOS_*                            */
+    float eos_param[2];        /* see BUBBLE_EOS_*                        */
 } bubble_spec;
 
 /* Config defaults (src/config.rs:197-297) as a SimulationSpec. */
 void bubble_spec_default(bubble_spec *out);
+
+/* Checks the spec's equation-of-state selection (policy, parameter ranges,
+ * supported arithmetic); BUBBLE_ERR_INVALID with a message otherwise. */
+int bubble_eos_validate(const bubble_spec *spec);
 
 /* ------------------------------------------------------------------------ */
 /*  Diagnostics (src/gpu/sim.rs:141-167, shaders/reduce.wgsl:15-79)          */

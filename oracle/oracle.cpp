@@ -191,8 +191,34 @@ inline vec4<R> eos_prim_from_cons_pert(const SimParams<R> &P, vec4<R> u) {
     return {zx / d, zy / d, zz / d, dp};
 }
 
-template <typename R, bool PERT = false>
+// Equation-of-state constants outside the reference's SimParams, set by
+// oracle_set_eos: the gamma law's c2 = Gamma - 1 and e0
+// (e = p / c2 + e0, docs/EOS.md:86-118) and the degrees-of-freedom ratio of
+// the phase-dependent radiation constant (docs/EOS.md:58-84).
+float g_eos_c2 = 0.0f, g_eos_e0 = 0.0f, g_eos_dof = 1.0f;
+
+// Gamma-law inversion: f(p) = p - c2 (E - Z^2 / (E + p) - e0) = 0 by a fixed
+// eight Newton steps from c2 (E - e0), floored at p_floor after each.
+template <typename R>
+inline vec4<R> eos_prim_from_cons_gamma(const SimParams<R> &P, vec4<R> u_raw) {
+    const vec4<R> u = eos_regularise(P, u_raw);
+    const R e_lab = u.x;
+    const R z2 = u.y * u.y + u.z * u.z + u.w * u.w;
+    const R c2 = R(g_eos_c2), e0 = R(g_eos_e0);
+    R p = wmax(c2 * (e_lab - e0), P.p_floor);
+    for (int it = 0; it < 8; ++it) {
+        const R sp = e_lab + p;
+        const R r = p - c2 * (e_lab - z2 / sp - e0);
+        const R d = R(1.0) - c2 * z2 / (sp * sp);
+        p = wmax(p - r / d, P.p_floor);
+    }
+    const R d = wmax(e_lab + p, R(1e-30));
+    return {u.y / d, u.z / d, u.w / d, p};
+}
+
+template <typename R, bool PERT = false, bool GAMMA = false>
 inline vec4<R> eos_prim_from_cons(const SimParams<R> &P, vec4<R> u_raw, R phi) {
+    if (GAMMA) return eos_prim_from_cons_gamma(P, u_raw);
     if (PERT) return eos_prim_from_cons_pert(P, u_raw);
     const vec4<R> u = eos_regularise(P, u_raw);
     const R e_lab = u.x;
@@ -203,12 +229,13 @@ inline vec4<R> eos_prim_from_cons(const SimParams<R> &P, vec4<R> u_raw, R phi) {
 }
 // PERT: the energy component is E - e_bg = w W^2 v^2 + 3 (p - p_bg); `w_out`
 // returns w W^2 for the energy flux w W^2 v_d.
-template <typename R, bool PERT = false>
+template <typename R, bool PERT = false, bool GAMMA = false>
 inline vec4<R> eos_cons_from_prim(const SimParams<R> &P, vec4<R> q, R phi, R *w_out = nullptr) {
     const R p = q.w;
     const R v2 = wmin(q.x * q.x + q.y * q.y + q.z * q.z, P.z_max * P.z_max);
     const R pf = PERT ? P.e_ref / R(3.0) + p : p;
-    const R w_gam2 = eos_enthalpy_from_pressure(pf, phi) / (R(1.0) - v2);
+    // gamma law: w = e + p = p / c2 + p + e0
+    const R w_gam2 = (GAMMA ? p / R(g_eos_c2) + p + R(g_eos_e0) : eos_enthalpy_from_pressure(pf, phi)) / (R(1.0) - v2);
     if (w_out) *w_out = w_gam2;
     if (PERT) return {w_gam2 * v2 + R(3.0) * p, w_gam2 * q.x, w_gam2 * q.y, w_gam2 * q.z};
     return {w_gam2 - p, w_gam2 * q.x, w_gam2 * q.y, w_gam2 * q.z};
@@ -229,11 +256,11 @@ inline vec4<R> eos_flux(vec4<R> q, vec4<R> u, int axis, R w = R(0)) {
     if (axis == 2) f.w = f.w + p;
     return f;
 }
-template <typename R>
+template <typename R, bool GAMMA = false>
 inline void eos_wave_speeds(const SimParams<R> &P, vec4<R> q, R phi, int axis, R &lm, R &lp) {
     const R v2 = wmin(q.x * q.x + q.y * q.y + q.z * q.z, P.z_max * P.z_max);
     const R vd = axis_comp(q, axis);
-    const R cs2 = eos_sound_speed2(q.w, phi);
+    const R cs2 = GAMMA ? R(g_eos_c2) : eos_sound_speed2(q.w, phi);
     const R cs = std::sqrt(cs2);
     const R denom = R(1.0) - v2 * cs2;
     const R rad = wmax((R(1.0) - v2) * (R(1.0) - vd * vd - cs2 * (v2 - vd * vd)), R(0.0));
@@ -261,16 +288,16 @@ inline vec4<R> sanitise(const SimParams<R> &P, vec4<R> q) {
     return {vx, vy, vz, p};
 }
 
-template <typename R, bool PERT = false>
+template <typename R, bool PERT = false, bool GAMMA = false>
 inline vec4<R> hll_flux(const SimParams<R> &P, vec4<R> q_l, R phi_l, vec4<R> q_r, R phi_r, int axis) {
     R w_l, w_r;
-    const vec4<R> u_l = eos_cons_from_prim<R, PERT>(P, q_l, phi_l, &w_l);
-    const vec4<R> u_r = eos_cons_from_prim<R, PERT>(P, q_r, phi_r, &w_r);
+    const vec4<R> u_l = eos_cons_from_prim<R, PERT, GAMMA>(P, q_l, phi_l, &w_l);
+    const vec4<R> u_r = eos_cons_from_prim<R, PERT, GAMMA>(P, q_r, phi_r, &w_r);
     const vec4<R> f_l = eos_flux<R, PERT>(q_l, u_l, axis, w_l);
     const vec4<R> f_r = eos_flux<R, PERT>(q_r, u_r, axis, w_r);
     R lml, lpl, lmr, lpr;
-    eos_wave_speeds(P, q_l, phi_l, axis, lml, lpl);
-    eos_wave_speeds(P, q_r, phi_r, axis, lmr, lpr);
+    eos_wave_speeds<R, GAMMA>(P, q_l, phi_l, axis, lml, lpl);
+    eos_wave_speeds<R, GAMMA>(P, q_r, phi_r, axis, lmr, lpr);
     const R s_min = wmin(wmin(lml, lmr), R(0.0));
     const R s_max = wmax(wmax(lpl, lpr), R(0.0));
     const R den = wmax(s_max - s_min, R(1e-12));
@@ -300,7 +327,7 @@ inline vec4<R> ld4(const R *a, size_t i) {
 }
 
 // step.wgsl main for one cell.
-template <typename R, bool PERT = false>
+template <typename R, bool PERT = false, bool GAMMA = false>
 void step_cell(const SimParams<R> &P, const StageParams<R> &S, const R *field_n, const R *fluid_n,
                const R *field_in, const R *fluid_in, const R *prim, R *field_out, R *fluid_out,
                int cx, int cy, int cz) {
@@ -328,9 +355,9 @@ void step_cell(const SimParams<R> &P, const StageParams<R> &S, const R *field_n,
         const vec4<R> slope_m1 = limit_slope4(sub(qm1, qm2), sub(q0, qm1));
         const vec4<R> slope_0 = limit_slope4(sub(q0, qm1), sub(qp1, q0));
         const vec4<R> slope_p1 = limit_slope4(sub(qp1, q0), sub(qp2, qp1));
-        const vec4<R> f_minus = hll_flux<R, PERT>(P, sanitise(P, add(qm1, scale(R(0.5), slope_m1))), phi_m,
+        const vec4<R> f_minus = hll_flux<R, PERT, GAMMA>(P, sanitise(P, add(qm1, scale(R(0.5), slope_m1))), phi_m,
                                          sanitise(P, sub(q0, scale(R(0.5), slope_0))), phi0, axis);
-        const vec4<R> f_plus = hll_flux<R, PERT>(P, sanitise(P, add(q0, scale(R(0.5), slope_0))), phi0,
+        const vec4<R> f_plus = hll_flux<R, PERT, GAMMA>(P, sanitise(P, add(q0, scale(R(0.5), slope_0))), phi0,
                                         sanitise(P, sub(qp1, scale(R(0.5), slope_p1))), phi_p, axis);
         flux_div = add(flux_div, scale(P.inv_dx, sub(f_plus, f_minus)));
     }
@@ -439,7 +466,7 @@ void nucleate_all(const SimParams<R> &P, const float *bubbles, uint32_t count, R
     }
 }
 
-template <typename R, bool PERT = false>
+template <typename R, bool PERT = false, bool GAMMA = false>
 void step_all(const SimParams<R> &P, const StageParams<R> &S, const R *field_n, const R *fluid_n,
               const R *field_in, const R *fluid_in, const R *prim, R *field_out, R *fluid_out) {
     const int nx = (int)P.nx, ny = (int)P.ny, nz = (int)P.nz;
@@ -447,15 +474,15 @@ void step_all(const SimParams<R> &P, const StageParams<R> &S, const R *field_n, 
     for (int z = 0; z < nz; ++z)
         for (int y = 0; y < ny; ++y)
             for (int x = 0; x < nx; ++x)
-                step_cell<R, PERT>(P, S, field_n, fluid_n, field_in, fluid_in, prim, field_out, fluid_out, x, y, z);
+                step_cell<R, PERT, GAMMA>(P, S, field_n, fluid_n, field_in, fluid_in, prim, field_out, fluid_out, x, y, z);
 }
 
-template <typename R, bool PERT = false>
+template <typename R, bool PERT = false, bool GAMMA = false>
 void primitives_all(const SimParams<R> &P, const R *field, const R *fluid, R *prim) {
     const size_t n = (size_t)P.nx * P.ny * P.nz;
 #pragma omp parallel for schedule(static)
     for (long long i = 0; i < (long long)n; ++i) {
-        const vec4<R> q = eos_prim_from_cons<R, PERT>(P, ld4(fluid, (size_t)i), field[2 * i]);
+        const vec4<R> q = eos_prim_from_cons<R, PERT, GAMMA>(P, ld4(fluid, (size_t)i), field[2 * i]);
         prim[4 * i] = q.x;
         prim[4 * i + 1] = q.y;
         prim[4 * i + 2] = q.z;
@@ -585,7 +612,13 @@ void vis_all(const SimParams<R> &P, const R *field, const R *fluid, const R *pri
         const R vv = vx * vx + vy * vy + vz * vz;
         const R speed = std::sqrt(vv);
         const R pt = PERT ? p_bg + wmax(q_w, P.p_floor) : wmax(p, P.p_floor);
-        const R x = R(3.0) * pt / P.a_rad;  // eos_temperature (shaders/eos.wgsl:65-69)
+        R a = P.a_rad;
+        if (g_eos_dof != 1.0f) {  // the phase-dependent radiation constant
+            const R h = wmin(wmax(phi / P.phi_b, R(0.0)), R(1.0));
+            const R smooth = h * h * (R(3.0) - R(2.0) * h);
+            a = P.a_rad * (R(1.0) + (R(g_eos_dof) - R(1.0)) * smooth);
+        }
+        const R x = R(3.0) * pt / a;  // eos_temperature (shaders/eos.wgsl:65-69)
         const R temp = std::sqrt(std::sqrt(x));
         const R kinetic = (e_lab + p) * vv;
         out[4 * i + 0] = f32_to_f16((float)(phi / P.phi_b));
@@ -944,6 +977,23 @@ void oracle_render(const float *view44, const uint16_t *tex, int nx, int ny, int
     render_all(V, T, width, height, out);
 }
 uint16_t oracle_f32_to_f16(float x) { return f32_to_f16(x); }
+
+// Equation of state of the following calls: c2 = Gamma - 1 and e0 of the
+// gamma law (used by the *_gamma_f32 kernels), and the degrees-of-freedom
+// ratio of the vis pack's temperature (1 = the bag model).
+void oracle_set_eos(float c2, float e0, float dof) {
+    g_eos_c2 = c2;
+    g_eos_e0 = e0;
+    g_eos_dof = dof;
+}
+void oracle_primitives_gamma_f32(const SimParams<float> *P, const float *field, const float *fluid, float *prim) {
+    primitives_all<float, false, true>(*P, field, fluid, prim);
+}
+void oracle_step_gamma_f32(const SimParams<float> *P, const StageParams<float> *S, const float *field_n,
+                           const float *fluid_n, const float *field_in, const float *fluid_in, const float *prim,
+                           float *field_out, float *fluid_out) {
+    step_all<float, false, true>(*P, *S, field_n, fluid_n, field_in, fluid_in, prim, field_out, fluid_out);
+}
 
 double oracle_tanh_f64(double x) { return oracle_tanh(x); }
 float oracle_tanh_f32(float x) { return oracle_tanh_r(x); }

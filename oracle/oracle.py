@@ -76,6 +76,9 @@ def lib() -> ctypes.CDLL:
         L.oracle_tanh_f32.argtypes = [ctypes.c_float]
         L.oracle_tanh_f32.restype = ctypes.c_float
         L.oracle_set_threads.argtypes = [ctypes.c_int]
+        L.oracle_set_eos.argtypes = [ctypes.c_float] * 3
+        L.oracle_primitives_gamma_f32.argtypes = [P, P, P, P]
+        L.oracle_step_gamma_f32.argtypes = [P] * 9
         L.oracle_render.argtypes = [P, P] + [ctypes.c_int] * 6 + [P]
         L.oracle_f32_to_f16.argtypes = [ctypes.c_float]
         L.oracle_f32_to_f16.restype = ctypes.c_uint16
@@ -321,10 +324,15 @@ def _ptr(a: np.ndarray) -> ctypes.c_void_p:
 class OracleSim:
     """CPU restatement of `Simulation` (src/gpu/sim.rs:180-1026)."""
 
-    def __init__(self, grid, model: dict | None = None, schedule=None, precision: str = "f32"):
+    def __init__(self, grid, model: dict | None = None, schedule=None, precision: str = "f32",
+                 eos: tuple = ("bag", 1.0, 0.0)):
         """precision: "f32", "f64", or "pert" (FP32 perturbation form: the
         fluid energy stored as E - e_ref, include/bubble.h
-        BUBBLE_PRECISION_PERTURBATION without its FP64 fallback)."""
+        BUBBLE_PRECISION_PERTURBATION without its FP64 fallback).
+        eos: ("bag", -, -), ("bag_dof", ratio, -) or ("gamma_law", Gamma, e0)
+        (include/bubble.h BUBBLE_EOS_*; the gamma law in FP32 only)."""
+        self.eos = (eos[0], f32(eos[1]), f32(eos[2]))
+        self.gamma = eos[0] == "gamma_law"
         self.model = dict(DEFAULT_MODEL, **(model or {}))
         err = validate(self.model)
         if err:
@@ -335,6 +343,7 @@ class OracleSim:
         self.dtype = np.float64 if precision == "f64" else np.float32
         self.sfx = "f64" if precision == "f64" else "f32"
         self.ksfx = "pert_f32" if self.pert else self.sfx  # kernels that differ in the perturbation form
+        self.gsfx = "gamma_f32" if self.gamma else self.ksfx  # kernels that differ for the gamma law
         self.d = derived(self.model)
         self.P = _sim_params(self.dtype, self.model, self.grid)
         self.field = np.zeros((3, self.n, 2), dtype=self.dtype)
@@ -377,14 +386,22 @@ class OracleSim:
 
     def stage(self, stage: int, in_slot: int, out_slot: int):
         L = lib()
+        self._set_eos()
         a0, a1 = (RK3_F32 if self.dtype == np.float32 else RK3_F64)[stage]
         S = np.array([a0, a1, self.d["dt"], 0.0], dtype=self.dtype)
-        getattr(L, f"oracle_primitives_{self.ksfx}")(_ptr(self.P), _ptr(self.field[in_slot]),
+        getattr(L, f"oracle_primitives_{self.gsfx}")(_ptr(self.P), _ptr(self.field[in_slot]),
                                                     _ptr(self.fluid[in_slot]), _ptr(self.prim))
-        getattr(L, f"oracle_step_{self.ksfx}")(
+        getattr(L, f"oracle_step_{self.gsfx}")(
             _ptr(self.P), _ptr(S), _ptr(self.field[self.cur]), _ptr(self.fluid[self.cur]),
             _ptr(self.field[in_slot]), _ptr(self.fluid[in_slot]), _ptr(self.prim),
             _ptr(self.field[out_slot]), _ptr(self.fluid[out_slot]))
+
+    def _set_eos(self):
+        kind, a, b = self.eos
+        c2 = f32(a - f32(1.0)) if kind == "gamma_law" else f32(0.0)
+        e0 = b if kind == "gamma_law" else f32(0.0)
+        dof = a if kind == "bag_dof" else f32(1.0)
+        lib().oracle_set_eos(float(c2), float(e0), float(dof))
 
     # record_step (src/gpu/sim.rs:881-916)
     def record_step(self):
@@ -413,7 +430,8 @@ class OracleSim:
         """The vis texture of the current slot as (nz, ny, nx, 4) uint16
         (binary16 bits of phi/phi_b, |v|, T/T_ref - 1, (E+p)v^2/e_ref)."""
         L = lib()
-        getattr(L, f"oracle_primitives_{self.ksfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
+        self._set_eos()
+        getattr(L, f"oracle_primitives_{self.gsfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
                                                     _ptr(self.fluid[self.cur]), _ptr(self.prim))
         nx, ny, nz = self.grid
         out = np.zeros((nz, ny, nx, 4), dtype=np.uint16)
@@ -424,7 +442,8 @@ class OracleSim:
     # record_visualisation's primitives pass + reduce (src/gpu/sim.rs:918-1010)
     def diagnostics(self) -> dict:
         L = lib()
-        getattr(L, f"oracle_primitives_{self.ksfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
+        self._set_eos()
+        getattr(L, f"oracle_primitives_{self.gsfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
                                                     _ptr(self.fluid[self.cur]), _ptr(self.prim))
         sums = np.zeros(4, dtype=np.float64)
         vmax = np.zeros(1, dtype=self.dtype)
