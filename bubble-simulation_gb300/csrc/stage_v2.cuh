@@ -24,11 +24,22 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "kernels.cuh"
 #include "tma.h"
 
 namespace bubble {
 namespace dev {
+
+// Compile-time loop: f(std::integral_constant<int, I>{}) for I = I0 .. N-1.
+template <int I0, int N, typename F>
+BUBBLE_DEV void static_for(F &&f) {
+    if constexpr (I0 < N) {
+        f(std::integral_constant<int, I0>{});
+        static_for<I0 + 1, N>(f);
+    }
+}
 
 BUBBLE_DEV uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -285,112 +296,160 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
     V2<R> pf{R(0), R(0)}, pfn{R(0), R(0)};
     V4<R> pu{R(0), R(0), R(0), R(0)}, pun{R(0), R(0), R(0), R(0)};
 
-    for (int z = z0;; ++z) {
-        // ---- phase X(z): combine plane z-1, face states of plane z --------
-        for (int k = t; k < L::X_TOTAL; k += NT) {
-            if (k < L::X_C) {
-                if (z == z0) continue;
-                const int zc = z - 1;
-                const int i = k % TX, j = k / TX;
-                if (i >= xe || j >= ye) continue;
-                const int c = (j + 2) * PW + (i + 2);
-                const R *ph0 = phi_slot(zc);
-                const R *phm = phi_slot(zc - 1);
-                const R *php = phi_slot(zc + 1);
-                const R phi0 = ph0[c], pi0 = pf.y;
-                const V4<R> q0 = prim_slot(zc)[c];
-                R lap_sum = R(0), gx, gy, gz;
-                {
-                    const R m = ph0[c - 1], p = ph0[c + 1];
-                    lap_sum = lap_sum + (m + p - R(2.0) * phi0);
-                    gx = R(0.5) * (p - m) * P.inv_dx;
-                }
-                {
-                    const R m = ph0[c - PW], p = ph0[c + PW];
-                    lap_sum = lap_sum + (m + p - R(2.0) * phi0);
-                    gy = R(0.5) * (p - m) * P.inv_dx;
-                }
-                {
-                    const R m = phm[c], p = php[c];
-                    lap_sum = lap_sum + (m + p - R(2.0) * phi0);
-                    gz = R(0.5) * (p - m) * P.inv_dx;
-                }
-                const V4<R> fxm = fxs[j * (TX + 1) + i], fxp = fxs[j * (TX + 1) + i + 1];
-                const V4<R> fym = fys[j * TX + i], fyp = fys[(j + 1) * TX + i];
-                const V4<R> fzm = fzs[((zc - 1 + 8) & 1) * NC + k], fzp = fzs[((zc + 8) & 1) * NC + k];
-                V4<R> fd;
-                if constexpr (FAST) {
-                    fd.x = ((fxp.x - fxm.x) + (fyp.x - fym.x) + (fzp.x - fzm.x)) * P.inv_dx;
-                    fd.y = ((fxp.y - fxm.y) + (fyp.y - fym.y) + (fzp.y - fzm.y)) * P.inv_dx;
-                    fd.z = ((fxp.z - fxm.z) + (fyp.z - fym.z) + (fzp.z - fzm.z)) * P.inv_dx;
-                    fd.w = ((fxp.w - fxm.w) + (fyp.w - fym.w) + (fzp.w - fzm.w)) * P.inv_dx;
-                } else {
-                    fd = V4<R>{R(0), R(0), R(0), R(0)};
-                    fd.x = fd.x + (fxp.x - fxm.x) * P.inv_dx;
-                    fd.y = fd.y + (fxp.y - fxm.y) * P.inv_dx;
-                    fd.z = fd.z + (fxp.z - fxm.z) * P.inv_dx;
-                    fd.w = fd.w + (fxp.w - fxm.w) * P.inv_dx;
-                    fd.x = fd.x + (fyp.x - fym.x) * P.inv_dx;
-                    fd.y = fd.y + (fyp.y - fym.y) * P.inv_dx;
-                    fd.z = fd.z + (fyp.z - fym.z) * P.inv_dx;
-                    fd.w = fd.w + (fyp.w - fym.w) * P.inv_dx;
-                    fd.x = fd.x + (fzp.x - fzm.x) * P.inv_dx;
-                    fd.y = fd.y + (fzp.y - fzm.y) * P.inv_dx;
-                    fd.z = fd.z + (fzp.z - fzm.z) * P.inv_dx;
-                    fd.w = fd.w + (fzp.w - fzm.w) * P.inv_dx;
-                }
-                const R laplacian = lap_sum * P.inv_dx * P.inv_dx;
-                const R vv = q0.x * q0.x + q0.y * q0.y + q0.z * q0.z;
-                R gam;
-                if constexpr (FAST) gam = rsqrt_approx(vmax(R(1.0) - vv, R(1e-12)));
-                else gam = R(1.0) / sqrt(vmax(R(1.0) - vv, R(1e-12)));
-                const R drag = P.eta * (gam * (pi0 + (q0.x * gx + q0.y * gy + q0.z * gz)));
-                const R d_pi = laplacian - dpotential(phi0, P) - drag;
-                const R dE = -fd.x + drag * pi0;
-                const R dZx = -fd.y - drag * gx;
-                const R dZy = -fd.z - drag * gy;
-                const R dZz = -fd.w - drag * gz;
-                const V2<R> fu{pf.x + A.dt * pi0, pf.y + A.dt * d_pi};
-                const V4<R> uu{pu.x + A.dt * dE, pu.y + A.dt * dZx, pu.z + A.dt * dZy, pu.w + A.dt * dZz};
-                const size_t g = (size_t)zc * plane + (size_t)(y0 + j) * P.nx + (x0 + i);
-                if (A.stage == 0) {
-                    A.field_out[g] = V2<R>{A.a1 * fu.x, A.a1 * fu.y};
-                    A.fluid_out[g] = V4<R>{A.a1 * uu.x, A.a1 * uu.y, A.a1 * uu.z, A.a1 * uu.w};
-                } else {
-                    A.field_out[g] = V2<R>{A.a0 * pfn.x + A.a1 * fu.x, A.a0 * pfn.y + A.a1 * fu.y};
-                    A.fluid_out[g] = V4<R>{A.a0 * pun.x + A.a1 * uu.x, A.a0 * pun.y + A.a1 * uu.y,
-                                           A.a0 * pun.z + A.a1 * uu.z, A.a0 * pun.w + A.a1 * uu.w};
-                }
-            } else if (z < z1) {
-                const int kk = k - L::X_C;
-                if (kk < L::X_Z) {
-                    V4<R> lo, hi;
-                    z_states(z + 1, kk, lo, hi);
-                    zlo[kk] = lo;
-                    zhi[((z + 1 + 8) & 1) * NC + kk] = hi;
-                } else if (kk < L::X_Z + L::X_Y) {
-                    const int q = kk - L::X_Z;
-                    const int jj = q / TX;  // cell row jj-1
-                    const int i = q - jj * TX;
-                    const int c = (jj + 1) * PW + (i + 2);
-                    const V4<R> *pr = prim_slot(z);
-                    V4<R> lo, hi;
-                    face_states<R, FAST>(pr[c - PW], pr[c], pr[c + PW], P.p_floor, zmax2, lo, hi);
-                    ylo[jj * TX + i] = lo;
-                    yhi[jj * TX + i] = hi;
-                } else {
-                    const int q = kk - L::X_Z - L::X_Y;
-                    const int j = q / (TX + 2);
-                    const int ii = q - j * (TX + 2);  // cell column ii-1
-                    const int c = (j + 2) * PW + (ii + 1);
-                    const V4<R> *pr = prim_slot(z);
-                    V4<R> lo, hi;
-                    face_states<R, FAST>(pr[c - 1], pr[c], pr[c + 1], P.p_floor, zmax2, lo, hi);
-                    xlo[j * (TX + 2) + ii] = lo;
-                    xhi[j * (TX + 2) + ii] = hi;
-                }
+    // ---- static work plan --------------------------------------------------
+    // Thread t takes the items k = t + r NT (r = 0, 1, ...) of each phase, the
+    // same on every plane.  The kinds of item are contiguous ranges of k, so
+    // the slot r meets only the kinds whose range intersects [r NT, (r+1) NT):
+    // with r unrolled those are known at compile time, and each item's indices
+    // are decoded once here instead of on every plane.
+    constexpr int NRX = (L::X_TOTAL + NT - 1) / NT;
+    constexpr int NRY = (L::Y_TOTAL + NT - 1) / NT;
+    // own cell of the combine (k = t < NC)
+    const int ci = t % TX, cj = t / TX;
+    const bool c_valid = t < NC && ci < xe && cj < ye;
+    const int cc = (cj + 2) * PW + (ci + 2);
+    const uint32_t c_off = (uint32_t)(y0 + cj) * (uint32_t)P.nx + (uint32_t)(x0 + ci);
+    // Y-phase primitive items: shared-memory cell of the cross-shaped halo
+    // layout, -1 outside the tile's cells
+    int ya_c[NRY];
+    static_for<0, NRY>([&](auto rc) {
+        constexpr int r = decltype(rc)::value;
+        ya_c[r] = -1;
+        if constexpr (r * NT < L::A_REAL) {
+            const int k = t + r * NT;
+            if (k < L::A_REAL) {
+                int i, j;
+                cross_item<TX, TY, PW>(k, i, j);
+                if (i < xe + 4 && j < ye + 4) ya_c[r] = j * PW + i;
             }
         }
+    });
+
+    for (int z = z0;; ++z) {
+        // ring slots of this plane, computed once for every item
+        const V4<R> *pr_zm1 = prim_slot(z - 1), *pr_z = prim_slot(z);
+        const V4<R> *pr_zp1 = prim_slot(z + 1), *pr_zp2 = prim_slot(z + 2);
+        const R *ph_zm2 = phi_slot(z - 2), *ph_zm1 = phi_slot(z - 1), *ph_z = phi_slot(z);
+        V4<R> *fz_rd_m = fzs + ((z - 2 + 8) & 1) * NC;   // face below plane z-1
+        V4<R> *fz_rd_p = fzs + ((z - 1 + 8) & 1) * NC;   // face above plane z-1
+        V4<R> *zhi_next = zhi + ((z + 1 + 8) & 1) * NC;
+        // ---- phase X(z): combine plane z-1, face states of plane z --------
+        static_for<0, NRX>([&](auto rc) {
+            constexpr int r = decltype(rc)::value;
+            constexpr int lo = r * NT, hi = (r + 1) * NT;
+            const int k = t + r * NT;
+            if constexpr (lo < L::X_C) {
+                if (k < L::X_C) {
+                    // combine plane zc = z-1 (k = t < NC)
+                    if (z == z0 || !c_valid) return;
+                    const int zc = z - 1;
+                    const int c = cc;
+                    const R phi0 = ph_zm1[c], pi0 = pf.y;
+                    const V4<R> q0 = pr_zm1[c];
+                    R lap_sum = R(0), gx, gy, gz;
+                    {
+                        const R m = ph_zm1[c - 1], p = ph_zm1[c + 1];
+                        lap_sum = lap_sum + (m + p - R(2.0) * phi0);
+                        gx = R(0.5) * (p - m) * P.inv_dx;
+                    }
+                    {
+                        const R m = ph_zm1[c - PW], p = ph_zm1[c + PW];
+                        lap_sum = lap_sum + (m + p - R(2.0) * phi0);
+                        gy = R(0.5) * (p - m) * P.inv_dx;
+                    }
+                    {
+                        const R m = ph_zm2[c], p = ph_z[c];
+                        lap_sum = lap_sum + (m + p - R(2.0) * phi0);
+                        gz = R(0.5) * (p - m) * P.inv_dx;
+                    }
+                    const V4<R> fxm = fxs[t + cj], fxp = fxs[t + cj + 1];
+                    const V4<R> fym = fys[t], fyp = fys[t + TX];
+                    const V4<R> fzm = fz_rd_m[t], fzp = fz_rd_p[t];
+                    V4<R> fd;
+                    if constexpr (FAST) {
+                        fd.x = ((fxp.x - fxm.x) + (fyp.x - fym.x) + (fzp.x - fzm.x)) * P.inv_dx;
+                        fd.y = ((fxp.y - fxm.y) + (fyp.y - fym.y) + (fzp.y - fzm.y)) * P.inv_dx;
+                        fd.z = ((fxp.z - fxm.z) + (fyp.z - fym.z) + (fzp.z - fzm.z)) * P.inv_dx;
+                        fd.w = ((fxp.w - fxm.w) + (fyp.w - fym.w) + (fzp.w - fzm.w)) * P.inv_dx;
+                    } else {
+                        fd = V4<R>{R(0), R(0), R(0), R(0)};
+                        fd.x = fd.x + (fxp.x - fxm.x) * P.inv_dx;
+                        fd.y = fd.y + (fxp.y - fxm.y) * P.inv_dx;
+                        fd.z = fd.z + (fxp.z - fxm.z) * P.inv_dx;
+                        fd.w = fd.w + (fxp.w - fxm.w) * P.inv_dx;
+                        fd.x = fd.x + (fyp.x - fym.x) * P.inv_dx;
+                        fd.y = fd.y + (fyp.y - fym.y) * P.inv_dx;
+                        fd.z = fd.z + (fyp.z - fym.z) * P.inv_dx;
+                        fd.w = fd.w + (fyp.w - fym.w) * P.inv_dx;
+                        fd.x = fd.x + (fzp.x - fzm.x) * P.inv_dx;
+                        fd.y = fd.y + (fzp.y - fzm.y) * P.inv_dx;
+                        fd.z = fd.z + (fzp.z - fzm.z) * P.inv_dx;
+                        fd.w = fd.w + (fzp.w - fzm.w) * P.inv_dx;
+                    }
+                    const R laplacian = lap_sum * P.inv_dx * P.inv_dx;
+                    const R vv = q0.x * q0.x + q0.y * q0.y + q0.z * q0.z;
+                    R gam;
+                    if constexpr (FAST) gam = rsqrt_approx(vmax(R(1.0) - vv, R(1e-12)));
+                    else gam = R(1.0) / sqrt(vmax(R(1.0) - vv, R(1e-12)));
+                    const R drag = P.eta * (gam * (pi0 + (q0.x * gx + q0.y * gy + q0.z * gz)));
+                    const R d_pi = laplacian - dpotential(phi0, P) - drag;
+                    const R dE = -fd.x + drag * pi0;
+                    const R dZx = -fd.y - drag * gx;
+                    const R dZy = -fd.z - drag * gy;
+                    const R dZz = -fd.w - drag * gz;
+                    const V2<R> fu{pf.x + A.dt * pi0, pf.y + A.dt * d_pi};
+                    const V4<R> uu{pu.x + A.dt * dE, pu.y + A.dt * dZx, pu.z + A.dt * dZy, pu.w + A.dt * dZz};
+                    const size_t g = (size_t)zc * plane + c_off;
+                    if (A.stage == 0) {
+                        A.field_out[g] = V2<R>{A.a1 * fu.x, A.a1 * fu.y};
+                        A.fluid_out[g] = V4<R>{A.a1 * uu.x, A.a1 * uu.y, A.a1 * uu.z, A.a1 * uu.w};
+                    } else {
+                        A.field_out[g] = V2<R>{A.a0 * pfn.x + A.a1 * fu.x, A.a0 * pfn.y + A.a1 * fu.y};
+                        A.fluid_out[g] = V4<R>{A.a0 * pun.x + A.a1 * uu.x, A.a0 * pun.y + A.a1 * uu.y,
+                                               A.a0 * pun.z + A.a1 * uu.z, A.a0 * pun.w + A.a1 * uu.w};
+                    }
+                    return;
+                }
+            }
+            if (z >= z1) return;
+            if constexpr (lo < L::X_C + L::X_Z && hi > L::X_C) {
+                if (k < L::X_C + L::X_Z) {
+                    // z face states of plane z+1 (cell n)
+                    const int n = k - L::X_C;
+                    const int c = (n / TX + 2) * PW + (n % TX + 2);
+                    V4<R> lo_s, hi_s;
+                    face_states<R, FAST>(pr_z[c], pr_zp1[c], pr_zp2[c], P.p_floor, zmax2, lo_s, hi_s);
+                    zlo[n] = lo_s;
+                    zhi_next[n] = hi_s;
+                    return;
+                }
+            }
+            if constexpr (lo < L::X_C + L::X_Z + L::X_Y && hi > L::X_C + L::X_Z) {
+                if (k < L::X_C + L::X_Z + L::X_Y) {
+                    // y face states of plane z, cell row jj-1
+                    const int q = k - L::X_C - L::X_Z;
+                    const int jj = q / TX;
+                    const int c = (jj + 1) * PW + (q - jj * TX + 2);
+                    V4<R> lo_s, hi_s;
+                    face_states<R, FAST>(pr_z[c - PW], pr_z[c], pr_z[c + PW], P.p_floor, zmax2, lo_s, hi_s);
+                    ylo[q] = lo_s;
+                    yhi[q] = hi_s;
+                    return;
+                }
+            }
+            if constexpr (hi > L::X_C + L::X_Z + L::X_Y) {
+                if (k < L::X_TOTAL) {
+                    // x face states of plane z, cell column ii-1
+                    const int q = k - L::X_C - L::X_Z - L::X_Y;
+                    const int j = q / (TX + 2);
+                    const int c = (j + 2) * PW + (q - j * (TX + 2) + 1);
+                    V4<R> lo_s, hi_s;
+                    face_states<R, FAST>(pr_z[c - 1], pr_z[c], pr_z[c + 1], P.p_floor, zmax2, lo_s, hi_s);
+                    xlo[q] = lo_s;
+                    xhi[q] = hi_s;
+                }
+            }
+        });
         if (z == z1) break;
         bool timed_out = false;
         if (z + 3 <= zlast) timed_out = !wait_plane(z + 3);
@@ -401,48 +460,60 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
         }
         // ---- phase Y(z): stage the next plane, primitives of z+3, fluxes ---
         if (z + 4 <= zlast) issue(z + 4);
-        if (t < NC) {
-            const int i = t % TX, j = t / TX;
-            if (i < xe && j < ye) {
-                const size_t g = (size_t)z * plane + (size_t)(y0 + j) * P.nx + (x0 + i);
-                pf = A.field_in[g];
-                pu = A.fluid_in[g];
-                if (A.stage != 0) {
-                    pfn = A.field_n[g];
-                    pun = A.fluid_n[g];
-                }
+        if (c_valid) {
+            const size_t g = (size_t)z * plane + c_off;
+            pf = A.field_in[g];
+            pu = A.fluid_in[g];
+            if (A.stage != 0) {
+                pfn = A.field_n[g];
+                pun = A.fluid_n[g];
             }
         }
         const bool do_a = z + 3 <= zlast;
-        for (int k = t; k < L::Y_TOTAL; k += NT) {
-            if (k < L::Y_A) {
-                if (!do_a || k >= L::A_REAL) continue;
-                int i, j;
-                cross_item<TX, TY, PW>(k, i, j);
-                if (i >= xe + 4 || j >= ye + 4) continue;
-                const int s = raw_slot(z + 3);
-                const int c = j * PW + i;
-                const V4<R> u = raw_u[s * PC + c];
-                phi_slot(z + 3)[c] = raw_f[s * PC + c].x;
-                prim_slot(z + 3)[c] = sanitise(recover<R, FAST, MIXED>(u, P), P.p_floor, zmax2);
-            } else {
-                const int kk = k - L::Y_A;
-                if (kk < L::Y_Z) {
-                    fzs[((z + 8) & 1) * NC + kk] = hll_flux<2, R, FAST, MIXED>(zhi[((z + 8) & 1) * NC + kk], zlo[kk], zmax2, P);
-                } else if (kk < L::Y_Z + L::Y_Y) {
-                    const int q = kk - L::Y_Z;
-                    const int f = q / TX;  // face between rows f-1 and f
-                    const int i = q - f * TX;
-                    fys[f * TX + i] = hll_flux<1, R, FAST, MIXED>(yhi[f * TX + i], ylo[(f + 1) * TX + i], zmax2, P);
-                } else {
-                    const int q = kk - L::Y_Z - L::Y_Y;
-                    const int j = q / (TX + 1);
-                    const int f = q - j * (TX + 1);  // face between columns f-1 and f
-                    fxs[j * (TX + 1) + f] =
-                        hll_flux<0, R, FAST, MIXED>(xhi[j * (TX + 2) + f], xlo[j * (TX + 2) + f + 1], zmax2, P);
+        V4<R> *pr_a = prim_slot(z + 3);
+        R *ph_a = phi_slot(z + 3);
+        const V4<R> *raw_ua = raw_u + raw_slot(z + 3) * PC;
+        const V2<R> *raw_fa = raw_f + raw_slot(z + 3) * PC;
+        V4<R> *fz_wr = fzs + ((z + 8) & 1) * NC;
+        const V4<R> *zhi_cur = zhi + ((z + 8) & 1) * NC;
+        static_for<0, NRY>([&](auto rc) {
+            constexpr int r = decltype(rc)::value;
+            constexpr int lo = r * NT, hi = (r + 1) * NT;
+            const int k = t + r * NT;
+            if constexpr (lo < L::Y_A) {
+                if (k < L::Y_A) {
+                    const int c = ya_c[r];
+                    if (!do_a || c < 0) return;
+                    const V4<R> u = raw_ua[c];
+                    ph_a[c] = raw_fa[c].x;
+                    pr_a[c] = sanitise(recover<R, FAST, MIXED>(u, P), P.p_floor, zmax2);
+                    return;
                 }
             }
-        }
+            if constexpr (lo < L::Y_A + L::Y_Z && hi > L::Y_A) {
+                if (k < L::Y_A + L::Y_Z) {
+                    const int kk = k - L::Y_A;
+                    fz_wr[kk] = hll_flux<2, R, FAST, MIXED>(zhi_cur[kk], zlo[kk], zmax2, P);
+                    return;
+                }
+            }
+            if constexpr (lo < L::Y_A + L::Y_Z + L::Y_Y && hi > L::Y_A + L::Y_Z) {
+                if (k < L::Y_A + L::Y_Z + L::Y_Y) {
+                    // face between rows f-1 and f: yhi[f*TX+i] = yhi[q], ylo[(f+1)*TX+i] = ylo[q+TX]
+                    const int q = k - L::Y_A - L::Y_Z;
+                    fys[q] = hll_flux<1, R, FAST, MIXED>(yhi[q], ylo[q + TX], zmax2, P);
+                    return;
+                }
+            }
+            if constexpr (hi > L::Y_A + L::Y_Z + L::Y_Y) {
+                if (k < L::Y_TOTAL) {
+                    // face between columns f-1 and f of row j: states j*(TX+2)+f and +1
+                    const int q = k - L::Y_A - L::Y_Z - L::Y_Y;
+                    const int j = q / (TX + 1);
+                    fxs[q] = hll_flux<0, R, FAST, MIXED>(xhi[q + j], xlo[q + j + 1], zmax2, P);
+                }
+            }
+        });
         __syncthreads();
     }
     return true;
