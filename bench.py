@@ -31,6 +31,7 @@ import argparse
 import json
 import math
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -185,11 +186,39 @@ def cpu_baseline(state, wl: dict, seconds_budget: float = 20.0) -> dict:
             break
     dt = time.perf_counter() - t0
     cells = nx * ny * zs
-    return {"value": cells * steps / dt, "unit": "cell-updates/s", "cores": oracle.lib().oracle_threads(),
-            "kind": "port",
+    threads = oracle.lib().oracle_threads()
+    # the same slab's first 8 planes on one thread
+    z1 = min(8, zs)
+    sim1 = oracle.OracleSim((nx, ny, z1), model=m)
+    sim1.set_state(field.reshape(nz, ny, nx, 2)[:z1].reshape(-1, 2), fluid.reshape(nz, ny, nx, 4)[:z1].reshape(-1, 4))
+    oracle.lib().oracle_set_threads(1)
+    t1 = time.perf_counter()
+    sim1.record_step()
+    dt1 = time.perf_counter() - t1
+    oracle.lib().oracle_set_threads(threads)
+    return {"value": cells * steps / dt, "unit": "cell-updates/s", "cores": threads,
+            "kind": "port", "value_1_thread": nx * ny * z1 / dt1, "cpu_model": cpu_model(),
+            "nproc": os.cpu_count(),
             "sample": f"{steps} SSP-RK3 step(s) of a {nx}x{ny}x{zs} periodic slab of the warmed-up "
                       f"{nx}x{ny}x{nz} state, FP32 oracle (reference kernel structure), "
-                      f"{oracle.lib().oracle_threads()} threads"}
+                      f"{threads} threads; value_1_thread: one step of its first {z1} planes on one thread"}
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (x86 'model name', Arm implementer/part)."""
+    try:
+        text = open("/proc/cpuinfo").read()
+    except OSError:
+        return platform.processor() or "unknown"
+    for key in ("model name", "Model name"):
+        for line in text.splitlines():
+            if line.startswith(key):
+                return line.split(":", 1)[1].strip()
+    impl = [ln.split(":", 1)[1].strip() for ln in text.splitlines() if ln.startswith("CPU implementer")]
+    part = [ln.split(":", 1)[1].strip() for ln in text.splitlines() if ln.startswith("CPU part")]
+    if impl and part:
+        return f"Arm implementer {impl[0]} part {part[0]} ({platform.machine()})"
+    return platform.processor() or platform.machine()
 
 
 def run_reference(args, wl: dict, world: int, rank: int) -> int:

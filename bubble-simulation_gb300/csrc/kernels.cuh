@@ -67,24 +67,59 @@ struct BubbleBatch {
     V4<float> b[kNucleateBatch];
 };
 
+// The launch covers the lattice in bricks of 32 x 8 x 8 cells, one CTA
+// each.  The CTA first keeps the bubbles that can reach its brick: a lower
+// bound of every cell's distance (per axis the circular distance of the
+// brick's centre minus its half extent -- the periodic distance is
+// 1-Lipschitz) whose tanh argument exceeds the cut-off by a margin rules a
+// bubble out, its profile being exactly 0 in the whole brick.  Every cell
+// then takes max(phi, 0), the far field of all the batch's bubbles, and the
+// maximum over the kept bubbles alone, in any order: the result equals the
+// reference's loop over the whole batch bit for bit.  A cell whose value
+// does not change is not written back.
+constexpr int kNucBx = 32, kNucBy = 8, kNucBz = 8;
+
 template <typename R>
-__global__ void nucleate_kernel(V2<R> *__restrict__ field, const __grid_constant__ BubbleBatch batch,
-                                LatticeParams<R> P) {
-    const uint64_t n = (uint64_t)P.nx * P.ny * P.nz;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    const R nxr = R(P.nx), nyr = R(P.ny), nzr = R(P.nz);
+__global__ void __launch_bounds__(256) nucleate_kernel(V2<R> *__restrict__ field,
+                                                        const __grid_constant__ BubbleBatch batch,
+                                                        LatticeParams<R> P) {
+    __shared__ int kept[kNucleateBatch];
+    __shared__ int n_kept;
+    const int bx = blockIdx.x * kNucBx, by = blockIdx.y * kNucBy, bz = blockIdx.z * kNucBz;
+    const int ex = min(kNucBx, P.nx - bx), ey = min(kNucBy, P.ny - by), ez = min(kNucBz, P.nz - bz);
+    if (threadIdx.x == 0) n_kept = 0;
+    __syncthreads();
     const R cut = TanhCut<R>::value;
-    const uint64_t xy = (uint64_t)P.nx * P.ny;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const int z = (int)(i / xy);
-        const int rem = (int)(i - (uint64_t)z * xy);
-        const int y = rem / P.nx;
-        const int x = rem - y * P.nx;
-        const R px = R(x), py = R(y), pz = R(z);
-        V2<R> f = field[i];
-        R phi = f.x;
-        for (int b = 0; b < batch.count; ++b) {
-            const V4<float> bub = batch.b[b];
+    for (int b = threadIdx.x; b < batch.count; b += blockDim.x) {
+        const V4<float> bub = batch.b[b];
+        const double c[3] = {(double)bub.x, (double)bub.y, (double)bub.z};
+        const int b0[3] = {bx, by, bz}, e[3] = {ex, ey, ez}, n[3] = {P.nx, P.ny, P.nz};
+        double lb2 = 0.0;
+        for (int a = 0; a < 3; ++a) {
+            const double half = 0.5 * (double)(e[a] - 1);
+            double d = (double)b0[a] + half - c[a];
+            if (d > 0.5 * n[a]) d -= n[a];
+            if (d < -0.5 * n[a]) d += n[a];
+            const double g = fmax(fabs(d) - half, 0.0);
+            lb2 += g * g;
+        }
+        const double arg_lb = (sqrt(lb2) * (double)P.dx - (double)bub.w * (double)P.dx) / (double)P.wall_width;
+        if (!(arg_lb > (double)cut + 0.25)) kept[atomicAdd(&n_kept, 1)] = b;
+    }
+    __syncthreads();
+    const int nk = n_kept;
+    const int tx = threadIdx.x % kNucBx, ty = threadIdx.x / kNucBx;
+    if (tx >= ex || ty >= ey) return;
+    const R nxr = R(P.nx), nyr = R(P.ny), nzr = R(P.nz);
+    const R px = R(bx + tx), py = R(by + ty);
+    for (int zz = 0; zz < ez; ++zz) {
+        const int z = bz + zz;
+        const size_t i = cell_index(bx + tx, by + ty, z, P);
+        const R phi0 = field[i].x;
+        R phi = vmax(phi0, R(0));
+        const R pz = R(z);
+        for (int q = 0; q < nk; ++q) {
+            const V4<float> bub = batch.b[kept[q]];
             const R dx = min_image(px - R(bub.x), nxr);
             const R dy = min_image(py - R(bub.y), nyr);
             const R dz = min_image(pz - R(bub.z), nzr);
@@ -94,8 +129,10 @@ __global__ void nucleate_kernel(V2<R> *__restrict__ field, const __grid_constant
             if (!(arg > cut)) profile = R(0.5) * P.phi_b * (R(1.0) - det_tanh_r<R>(arg));
             phi = vmax(phi, profile);
         }
-        f.x = phi;
-        field[i] = f;
+        bool same;
+        if constexpr (sizeof(R) == 4) same = __float_as_uint((float)phi) == __float_as_uint((float)phi0);
+        else same = __double_as_longlong((double)phi) == __double_as_longlong((double)phi0);
+        if (!same) field[i].x = phi;
     }
 }
 

@@ -55,13 +55,14 @@ cudaError_t init(V2<R> *field, V4<R> *fluid, uint64_t n, R e_ref, cudaStream_t s
 template <typename R>
 cudaError_t nucleate(V2<R> *field, const V4<float> *bubbles, int count, const LatticeParams<R> &P,
                      cudaStream_t s) {
-    const uint64_t n = (uint64_t)P.nx * P.ny * P.nz;
+    const dim3 grid((unsigned)((P.nx + dev::kNucBx - 1) / dev::kNucBx), (unsigned)((P.ny + dev::kNucBy - 1) / dev::kNucBy),
+                    (unsigned)((P.nz + dev::kNucBz - 1) / dev::kNucBz));
     for (int first = 0; first < count; first += dev::kNucleateBatch) {
         dev::BubbleBatch batch;
         batch.count = count - first < dev::kNucleateBatch ? count - first : dev::kNucleateBatch;
         batch._pad[0] = batch._pad[1] = batch._pad[2] = 0;
         for (int k = 0; k < batch.count; ++k) batch.b[k] = bubbles[first + k];
-        dev::nucleate_kernel<R><<<grid_for(n, 256), 256, 0, s>>>(field, batch, P);
+        dev::nucleate_kernel<R><<<grid, dev::kNucBx * dev::kNucBy, 0, s>>>(field, batch, P);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }

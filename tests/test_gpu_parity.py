@@ -182,6 +182,34 @@ def test_nucleation_bit_exact(bubble, gpu, oracle_mod, precision):
 
 
 @pytest.mark.parametrize("precision", ["single", "double"])
+def test_nucleation_culling_bit_exact(bubble, gpu, oracle_mod, precision):
+    """The brick-culled nucleation kernel against the oracle's loop over the
+    whole batch: 300 bubbles (three launches of <= 128), a grid that is no
+    multiple of the 32 x 8 x 8 brick, small radii so most bricks keep few
+    bubbles, and a field that is negative everywhere beforehand, so the max
+    with the far field (exactly 0) must reach every cell."""
+    grid = (45, 37, 29)
+    p = "f32" if precision == "single" else "f64"
+    sched = oracle_mod.make_schedule("simultaneous", 300, 2.0, grid, 1.0, 11)
+    o = oracle_mod.OracleSim(grid, schedule=sched, precision=p)
+    f0, u0 = o.state()
+    rng = np.random.default_rng(3)
+    f0 = f0.copy()
+    f0[:, 0] = -np.abs(rng.standard_normal(len(f0))).astype(f0.dtype) * f0.dtype.type(0.01)
+    o.set_state(f0, u0)
+    o.record_nucleation()
+    spec = spec_for(bubble, grid, precision, nucleation="simultaneous", bubbles=300,
+                    model=bubble.Model(seed_kind="cells", seed_value=2.0), seed=11)
+    with bubble.Simulation(spec) as sim:
+        sim.load_state(f0, u0)
+        sim.record_steps(0)
+        f, _ = sim.copy_state()
+    fo, _ = o.state()
+    assert_bit_equal(f, fo, "nucleated field")
+    assert (f[:, 0] >= 0).all()
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
 def test_diagnostics_match_oracle(bubble, gpu, golden, oracle_mod, precision):
     case = "tile_partial"
     p = "f32" if precision == "single" else "f64"
