@@ -516,6 +516,9 @@ int Batch::advance(uint64_t steps, std::string &err) {
         uint64_t k = steps - done;
         for (const auto &L : lats_)
             if (L.state) k = std::min(k, steps_until_event(L, k));
+        // the kernel numbers the grabs of a launch's rounds in 32 bits
+        k = std::min<uint64_t>(
+            k, std::max<uint64_t>(1, 0x7fffffffull / (3ull * (uint64_t)(std::max(n_items_, 1) + grid_))));
         const int rc = launch_chunk(k, err);
         if (rc != BUBBLE_OK) return rc;
         for (auto &L : lats_) {
@@ -530,12 +533,15 @@ int Batch::advance(uint64_t steps, std::string &err) {
 }
 
 int Batch::check_status(std::string &err) {
-    int st = 0;
-    BATCH_CUDA(cudaMemcpyAsync(&st, d_status_, sizeof(int), cudaMemcpyDeviceToHost, stream_), "status readback");
+    int st[16] = {0};
+    BATCH_CUDA(cudaMemcpyAsync(st, d_status_, sizeof(st), cudaMemcpyDeviceToHost, stream_), "status readback");
     BATCH_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
-    if (st != 0) {
-        BATCH_CUDA(cudaMemsetAsync(d_status_, 0, sizeof(int), stream_), "cudaMemset");
-        err = "a batch launch gave up on a bounded wait (status " + std::to_string(st) + ")";
+    if (st[0] != 0) {
+        BATCH_CUDA(cudaMemsetAsync(d_status_, 0, sizeof(st), stream_), "cudaMemset");
+        err = "a batch launch gave up on a bounded wait (status " + std::to_string(st[0]) + ")";
+        if (st[8])
+            err += "; stage wait gave up in item " + std::to_string(st[9]) + " (lattice " + std::to_string(st[10]) +
+                   ", round " + std::to_string(st[11]) + ", local item " + std::to_string(st[12]) + ")";
         return BUBBLE_ERR_TIMEOUT;
     }
     return BUBBLE_OK;

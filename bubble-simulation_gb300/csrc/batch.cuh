@@ -61,7 +61,6 @@ __global__ void __launch_bounds__(V2Layout<float, TY>::NT, V2Layout<float, TY>::
                     unsigned int *counters, int *status) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int item_s;
-    const float rk[3][2] = {{0.0f, 1.0f}, {0.75f, 0.25f}, {1.0f / 3.0f, 2.0f / 3.0f}};
     unsigned int round = 0;
     // Every CTA ends a round with one grab past the last item, so a round
     // consumes exactly n_items + gridDim.x grabs of the counter.
@@ -95,14 +94,23 @@ __global__ void __launch_bounds__(V2Layout<float, TY>::NT, V2Layout<float, TY>::
                 A.fluid_in = B.fluid[in_slot];
                 A.field_out = B.field[out_slot];
                 A.fluid_out = B.fluid[out_slot];
-                A.a0 = rk[stage][0];
-                A.a1 = rk[stage][1];
+                // the RK3 table (src/gpu/sim.rs:133-135) as selects, not an indexed array
+                A.a0 = stage == 0 ? 0.0f : (stage == 1 ? 0.75f : 1.0f / 3.0f);
+                A.a1 = stage == 0 ? 1.0f : (stage == 1 ? 0.25f : 2.0f / 3.0f);
                 A.dt = B.dt;
                 A.stage = stage;
                 const LatticeParams<float> P = B.P;
                 if (!v2_item<float, FAST, false, TY>(smem, A, P, B.lz, &B.maps[in_slot], B.tma_ok, status,
-                                                     local % B.tiles_xy, local / B.tiles_xy))
+                                                     local % B.tiles_xy, local / B.tiles_xy)) {
+                    // record where the stage's bounded wait gave up (status[8..12])
+                    if (threadIdx.x == 0 && atomicCAS(&status[8], 0, 1) == 0) {
+                        status[9] = item;
+                        status[10] = lo;
+                        status[11] = (int)round;
+                        status[12] = local;
+                    }
                     return;
+                }
             }
             if (!grid_barrier(&counters[0], &counters[1], status)) return;
         }

@@ -568,18 +568,79 @@ template <typename R>
 struct TanhCut;
 template <>
 struct TanhCut<float> {
-    static constexpr float value = 12.0f;
+    static constexpr float value = 9.5f;
 };
 template <>
 struct TanhCut<double> {
     static constexpr double value = 22.0;
 };
 
+// Deterministic FP32 tanh of the FP32 nucleation profile:
+// tanh|x| = m / (m + 2) with m = expm1(2|x|); expm1(y) from its Taylor series
+// to y^8/8! for y < ln2/2, else by Cody-Waite reduction y = k ln2 + r (ln2 split
+// so that k ln2_hi is exact) as 2^k expm1(r) + (2^k - 1).  Only IEEE +, -, *,
+// / rounded to nearest (explicit on the device, so no FMA contraction whatever
+// the flags) and exact operations (rint, ldexp, copysign): the CPU oracle gets
+// the same bits.  Beyond |x| = 9.5 it returns +-1 exactly, which is what a
+// correctly rounded tanhf returns there (1 - tanh(9.5) < 2^-25).  Error below
+// 4 ulp against libm (tested).
+BUBBLE_HD float f32_add(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+BUBBLE_HD float f32_mul(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+BUBBLE_HD float f32_div(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fdiv_rn(a, b);
+#else
+    return a / b;
+#endif
+}
+BUBBLE_HD float expm1_taylor_f32(float y) {
+    float t = 2.48015873e-05f;  // 1/8!
+    t = f32_add(1.98412698e-04f, f32_mul(y, t));
+    t = f32_add(1.38888889e-03f, f32_mul(y, t));
+    t = f32_add(8.33333333e-03f, f32_mul(y, t));
+    t = f32_add(4.16666667e-02f, f32_mul(y, t));
+    t = f32_add(1.66666667e-01f, f32_mul(y, t));
+    t = f32_add(0.5f, f32_mul(y, t));
+    t = f32_add(1.0f, f32_mul(y, t));
+    return f32_mul(y, t);
+}
+BUBBLE_HD float det_tanh_f32(float x) {
+    const float a = fabsf(x);
+    if (a > 9.5f) return copysignf(1.0f, x);
+    const float y = f32_add(a, a);
+    float m;
+    if (y < 0.346573590f) {
+        m = expm1_taylor_f32(y);
+    } else {
+        const float k = rintf(f32_mul(y, 1.44269504f));
+        const float r = f32_add(f32_add(y, -f32_mul(k, 0.693145752f)), -f32_mul(k, 1.42860677e-06f));
+        const float p2 = ldexpf(1.0f, (int)k);
+        m = f32_add(f32_mul(p2, expm1_taylor_f32(r)), f32_add(p2, -1.0f));
+    }
+    return copysignf(f32_div(m, f32_add(m, 2.0f)), x);
+}
+
 template <typename R>
 BUBBLE_HD R det_tanh_r(R x) {
-    if (x > TanhCut<R>::value) return R(1);
-    if (x < -TanhCut<R>::value) return R(-1);
-    return (R)det_tanh((double)x);
+    if constexpr (sizeof(R) == 4) {
+        return det_tanh_f32(x);
+    } else {
+        if (x > TanhCut<R>::value) return R(1);
+        if (x < -TanhCut<R>::value) return R(-1);
+        return det_tanh(x);
+    }
 }
 
 // min_image (shaders/nucleate.wgsl:51-57).

@@ -423,10 +423,37 @@ inline double oracle_tanh(double x) {
     }
     return x < 0.0 ? -t : t;
 }
+// FP32 tanh for the FP32 profile: tanh|x| = m / (m + 2), m = expm1(2|x|),
+// expm1 from its Taylor series to y^8/8! below ln2/2, else by Cody-Waite
+// reduction y = k ln2_hi + k ln2_lo + r and 2^k expm1(r) + (2^k - 1); +-1
+// beyond |x| = 9.5 (where tanhf rounds to 1).  Single-precision IEEE
+// operations in a fixed order (-ffp-contract=off), as the CUDA library
+// evaluates them.
+inline float oracle_expm1_f32(float y) {
+    float t = 2.48015873e-05f;
+    t = 1.98412698e-04f + y * t;
+    t = 1.38888889e-03f + y * t;
+    t = 8.33333333e-03f + y * t;
+    t = 4.16666667e-02f + y * t;
+    t = 1.66666667e-01f + y * t;
+    t = 0.5f + y * t;
+    t = 1.0f + y * t;
+    return y * t;
+}
 inline float oracle_tanh_r(float x) {
-    if (x > 12.0f) return 1.0f;
-    if (x < -12.0f) return -1.0f;
-    return (float)oracle_tanh((double)x);
+    const float a = std::fabs(x);
+    if (a > 9.5f) return std::copysign(1.0f, x);
+    const float y = a + a;
+    float m;
+    if (y < 0.346573590f) {
+        m = oracle_expm1_f32(y);
+    } else {
+        const float k = std::rint(y * 1.44269504f);
+        const float r = (y + -(k * 0.693145752f)) + -(k * 1.42860677e-06f);
+        const float p2 = std::ldexp(1.0f, (int)k);
+        m = p2 * oracle_expm1_f32(r) + (p2 + -1.0f);
+    }
+    return std::copysign(m / (m + 2.0f), x);
 }
 inline double oracle_tanh_r(double x) { return oracle_tanh(x); }
 

@@ -143,9 +143,22 @@ def test_oracle_tanh_is_accurate(oracle_mod):
         t = L.oracle_tanh_f64(float(x))
         ref = math.tanh(float(x))
         assert abs(t - ref) <= 1e-15 * max(abs(ref), 1e-300), (x, t, ref)
-    for x in np.linspace(-14, 14, 2001).astype(np.float32):
-        t = L.oracle_tanh_f32(float(x))
-        assert abs(t - math.tanh(float(x))) <= 1.2e-7, x
+    # the FP32 tanh of the FP32 profile: within 4 ulp of the exact value, and
+    # exactly +-1 where a correctly rounded tanhf is
+    rng = np.random.default_rng(0)
+    xs = np.concatenate([np.linspace(-14, 14, 20001), rng.uniform(-10, 10, 20000),
+                         np.geomspace(1e-30, 1.0, 400), -np.geomspace(1e-30, 1.0, 400)]).astype(np.float32)
+    worst = 0.0
+    for x in xs:
+        t = np.float32(L.oracle_tanh_f32(float(x)))
+        ref = math.tanh(float(x))
+        ulp = float(np.spacing(np.float32(abs(ref)))) if ref != 0.0 else 1e-45
+        err = abs(float(t) - ref) / ulp
+        worst = max(worst, err)
+        assert err <= 4.0, (x, t, ref, err)
+        if abs(float(x)) > 9.5:
+            assert abs(float(t)) == 1.0
+    assert worst > 0.0
 
 
 # docs/NUMERICS.md:163-175: the quiescent state is a discrete fixed point
