@@ -204,6 +204,19 @@ def cpu_baseline(state, wl: dict, seconds_budget: float = 20.0) -> dict:
                       f"{threads} threads; value_1_thread: one step of its first {z1} planes on one thread"}
 
 
+def max_over_ranks(ms: float, dist, device: str) -> float:
+    """The whole job's clock: the slowest rank's time (ms).  `dist` is
+    torch.distributed (None for one rank); `device` holds the reduced tensor
+    ("cuda" under NCCL, "cpu" under gloo)."""
+    if dist is None:
+        return ms
+    import torch
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def cpu_model() -> str:
     """The host CPU's model name (x86 'model name', Arm implementer/part)."""
     try:
@@ -479,11 +492,7 @@ def main() -> int:
         end.synchronize()
     barrier()
     launches = sim.launches() - launches0
-    ms = start.elapsed_time(end)
-    if pg:
-        t = torch.tensor([ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(start.elapsed_time(end), pg, "cuda")
     ms_per_step = ms / args.steps
     value = world * cells * args.steps / (ms * 1e-3)
 
