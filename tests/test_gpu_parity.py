@@ -181,6 +181,27 @@ def test_nucleation_bit_exact(bubble, gpu, oracle_mod, precision):
     assert (f[:, 0] > 0.5).sum() > 0
 
 
+@pytest.mark.parametrize("grid", [(8, 8, 8), (2048, 8, 8), (8, 2048, 8), (8, 8, 2048), (33, 9, 200)])
+def test_extreme_shapes_bit_exact(bubble, gpu, oracle_mod, grid):
+    """The axis limits (8 and 2048 cells) and lopsided boxes: the smallest
+    lattice the 5-point stencil allows, one 2048-cell axis with the others at
+    the minimum (one x tile of 2048 columns; 256 y tiles; one column of 2048
+    planes), and an odd shape no tile divides.  Strict FP32 and FP64 against
+    the oracle, bit for bit, after nucleation and 4 steps."""
+    for prec, p in (("single", "f32"), ("double", "f64")):
+        sched = oracle_mod.make_schedule("simultaneous", 2, 3.0, grid, 1.0, 4)
+        o = oracle_mod.OracleSim(grid, schedule=sched, precision=p)
+        o.advance(4)
+        fo, uo = o.state()
+        spec = spec_for(bubble, grid, prec, nucleation="simultaneous", bubbles=2,
+                        model=bubble.Model(seed_kind="cells", seed_value=3.0), seed=4)
+        with bubble.Simulation(spec) as sim:
+            sim.advance(4)
+            f, u = sim.copy_state()
+        assert_bit_equal(f, fo, f"{p} field {grid}")
+        assert_bit_equal(u, uo, f"{p} fluid {grid}")
+
+
 @pytest.mark.parametrize("precision", ["single", "double"])
 def test_nucleation_culling_bit_exact(bubble, gpu, oracle_mod, precision):
     """The brick-culled nucleation kernel against the oracle's loop over the
