@@ -61,7 +61,7 @@ def test_batch_equals_plain_strict(bubble, gpu, events):
 
 
 def test_batch_fast_outcomes_match_plain(bubble, gpu):
-    """BASELINE's batched ensemble in miniature: grow/collapse outcome of each
+    """The batched-ensemble workload in miniature: grow/collapse outcome of each
     run equals the plain path's, fields within 1e-4 after 300 steps."""
     specs = mixed_specs(bubble, 8, "fast", seed=11)
     steps = 300
