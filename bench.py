@@ -1,7 +1,7 @@
 """Benchmark of the GB300 lattice time step.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload precision512|default128|plain64]
+                    [--workload precision512|default128|plain64|profile256|batch64|serve|precision_study]
 
 Metric: cell-updates/s (one cell-update = one full SSP-RK3 step of one
 cell), on the 512^3 precision-study workload by default: periodic 512^3
@@ -430,6 +430,73 @@ def run_serve(args) -> int:
     return 0
 
 
+def run_precision_study(args) -> int:
+    """The precision-study configuration against the FP64 CUDA oracle: the same
+    seeded lattice (edge --study-grid, the 512^3 config's bubble density, eta
+    drawn as in precision512) advanced --study-steps steps in FP64 (DOUBLE),
+    FP32 MIXED and the FP32 perturbation form.  Every 100 steps the total
+    energy (FP64 sums); drift = E / E0 - 1 with E0 the first report after
+    every bubble is in (src/headless.rs:69-75); at the end, per-field max
+    error of each FP32 form against FP64, relative to the field's FP64 max."""
+    import numpy as np
+    import torch
+    import bubble_gb300 as bubble
+
+    bubble.load()
+    n, steps = args.study_grid, args.study_steps
+    wl = workload("precision512")
+    bubbles = max(1, round(256 * (n / 512) ** 3))
+    model = bubble.Model(eta=wl["eta"])
+    out, states = {}, {}
+    for prec in ("double", "mixed", "perturbation"):
+        spec = bubble.SimulationSpec(model=model, grid=(n, n, n), nucleation="simultaneous", bubbles=bubbles,
+                                     nucleation_duration=1.0, seed=wl["seed"], precision=prec, math="fast")
+        series, e0 = [], None
+        t0 = time.perf_counter()
+        with bubble.Simulation(spec) as sim:
+            done = 0
+            while done < steps:
+                k = min(100, steps - done)
+                sim.advance(k)
+                done += k
+                d = sim.diagnostics()
+                if e0 is None and sim.remaining_bubbles() == 0:
+                    e0 = d.mean_energy_f64
+                series.append({"step": done, "mean_energy_f64": d.mean_energy_f64,
+                               "drift": (d.mean_energy_f64 / e0 - 1.0) if e0 else None,
+                               "broken": d.broken_fraction, "max_v": d.max_velocity})
+            f, u = sim.copy_state()
+        torch.cuda.synchronize()
+        if prec == "perturbation":
+            u = u.astype(np.float64)
+            u[:, 0] += float(bubble.derived(model)["e_ref"])
+        states[prec] = (f.astype(np.float64), u.astype(np.float64))
+        out[prec] = {"seconds": time.perf_counter() - t0, "series": series}
+    f64, u64 = states["double"]
+    names = ("phi", "pi", "E", "Zx", "Zy", "Zz")
+    for prec in ("mixed", "perturbation"):
+        f, u = states[prec]
+        err = {}
+        for c, nm in enumerate(names):
+            a = f[:, c] if c < 2 else u[:, c - 2]
+            b = f64[:, c] if c < 2 else u64[:, c - 2]
+            err[nm] = float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+        e = u64[:, 0] - float(bubble.derived(model)["e_ref"])
+        err["E - e_ref"] = float(np.abs((u[:, 0] - float(bubble.derived(model)["e_ref"])) - e).max()
+                                 / max(np.abs(e).max(), 1e-300))
+        out[prec]["field_err_vs_fp64"] = err
+        d32 = out[prec]["series"][-1]["drift"]
+        d64 = out["double"]["series"][-1]["drift"]
+        out[prec]["final_drift"] = d32
+        out[prec]["drift_minus_fp64_drift"] = d32 - d64
+    line = {"metric": "energy drift and per-field error vs the FP64 CUDA oracle", "impl": "gb300-precision-study",
+            "config": {"workload": f"{n}^3 periodic, {bubbles} bubbles at t=0 (1.15 R_c), eta {wl['eta']:.4f}, "
+                                   f"{steps} steps, fast arithmetic", "grid": [n, n, n]},
+            "final_drift_fp64": out["double"]["series"][-1]["drift"], "forms": out}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -442,12 +509,16 @@ def main() -> int:
     ap.add_argument("--lattices", type=int, default=64, help="batch64 workload: number of lattices")
     ap.add_argument("--batch-steps", type=int, default=1000, help="batch64 workload: steps per solve")
     ap.add_argument("--requests", type=int, default=24, help="serve workload: number of requests")
+    ap.add_argument("--study-grid", type=int, default=256, help="precision_study workload: lattice edge")
+    ap.add_argument("--study-steps", type=int, default=3000, help="precision_study workload: steps")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.workload == "batch64":
         return run_batch(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.workload == "precision_study":
+        return run_precision_study(args)
     wl = workload(args.workload)
     world, rank, local = dist_setup()
 

@@ -104,6 +104,27 @@ def test_stage_slots(bubble, oracle_mod):
 
 
 # src/gpu/sim.rs:1108-1116
+def test_rk3_third_stage_weights_do_not_sum_to_one_in_binary32(bubble):
+    """The origin of the FP32 scheme's systematic drift: the reference's third
+    stage weights fl(1/3) + fl(2/3) sum to exactly 1 + 2^-25 in binary32 (the
+    other stages' weights are exact), so over evolving cells a0 U^n + a1 U1
+    comes out 2.98e-8 too large on average (round to nearest of a biased
+    value).  The fast kernels evaluate U^n + a1 (U1 - U^n), unbiased."""
+    (a0, a1), (b0, b1), (c0, c1) = [tuple(map(np.float32, p)) for p in bubble.rk3_coefficients()]
+    assert float(a0) + float(a1) == 1.0 and float(b0) + float(b1) == 1.0
+    assert float(c0) + float(c1) == 1.0 + 2.0 ** -25
+    rng = np.random.default_rng(0)
+    un = rng.uniform(0.12, 0.13, 200_000).astype(np.float32)
+    u1 = (un * (1.0 + rng.normal(0.0, 1e-4, un.size))).astype(np.float32)
+    exact = un.astype(np.float64) / 3.0 + u1.astype(np.float64) * (2.0 / 3.0)
+    biased = (c0 * un).astype(np.float32) + (c1 * u1).astype(np.float32)
+    unbiased = un + (c1 * (u1 - un)).astype(np.float32)
+    rel_b = np.mean(biased.astype(np.float64) / exact - 1.0)
+    rel_u = np.mean(unbiased.astype(np.float64) / exact - 1.0)
+    assert abs(rel_b - 2.0 ** -25) < 0.2 * 2.0 ** -25, rel_b
+    assert abs(rel_u) < 0.05 * 2.0 ** -25, rel_u
+
+
 def test_rk3(bubble, oracle_mod):
     for (a0, a1), (b0, b1) in zip(bubble.rk3_coefficients(), oracle_mod.RK3_F32):
         assert f32(a0) == b0 and f32(a1) == b1
