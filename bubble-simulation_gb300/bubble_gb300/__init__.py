@@ -125,6 +125,7 @@ class SimulationSpec:
     precision: str = "single"  # single | mixed | double | perturbation
     math: str = "fast"  # fast | strict
     eos: str = "bag"  # bag | bag_dof (eos_param = (dof ratio, -)) | gamma_law (eos_param = (Gamma, e0))
+    #                   | thermal (eos_param = (gamma, A) of the temperature-dependent potential)
     eos_param: tuple = (1.0, 0.0)
 
     def c(self) -> _lib.Spec:

@@ -27,7 +27,7 @@ SEED_CELLS = 1
 NUCLEATION = {"simultaneous": 0, "exponential": 1, "centre": 2, "uniform": 3}
 PRECISION = {"single": 0, "mixed": 1, "double": 2, "perturbation": 3}
 MATH = {"fast": 0, "strict": 1}
-EOS = {"bag": 0, "bag_dof": 1, "gamma_law": 2}
+EOS = {"bag": 0, "bag_dof": 1, "gamma_law": 2, "thermal": 3}
 PATH_FUSED = 0
 PATH_REFERENCE = 1
 PATH_FUSED_SYNC = 2

@@ -56,7 +56,7 @@ std::string check_spec(const bubble_spec &s, int math) {
     const std::string msg = validate_model(s.model);
     if (!msg.empty()) return msg;
     if (s.precision != BUBBLE_PRECISION_SINGLE) return "a batch runs FP32 lattices (BUBBLE_PRECISION_SINGLE)";
-    if (s.eos == BUBBLE_EOS_GAMMA_LAW) return "a batch runs the bag equation of state";
+    if (s.eos == BUBBLE_EOS_GAMMA_LAW || s.eos == BUBBLE_EOS_THERMAL) return "a batch runs the bag equation of state";
     if (s.math != math) return "all lattices of a batch share one math mode";
     for (int a = 0; a < 3; ++a)
         if (s.grid[a] < BUBBLE_MIN_GRID || s.grid[a] > BUBBLE_MAX_GRID) return "grid axis out of 8..2048";

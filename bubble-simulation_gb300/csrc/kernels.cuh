@@ -484,10 +484,12 @@ __global__ void __launch_bounds__(TX *(TY + 1))
                 } else {
                     const V2<R> fn = A.field_n[g];
                     const V4<R> un = A.fluid_n[g];
-                    A.field_out[g] = V2<R>{A.a0 * fn.x + A.a1 * fu.x, A.a0 * fn.y + A.a1 * fu.y};
-                    A.fluid_out[g] =
-                        V4<R>{A.a0 * un.x + A.a1 * uu.x, A.a0 * un.y + A.a1 * uu.y,
-                              A.a0 * un.z + A.a1 * uu.z, A.a0 * un.w + A.a1 * uu.w};
+                    A.field_out[g] = V2<R>{rk_combine<R, FAST>(A.a0, A.a1, fn.x, fu.x),
+                                           rk_combine<R, FAST>(A.a0, A.a1, fn.y, fu.y)};
+                    A.fluid_out[g] = V4<R>{rk_combine<R, FAST>(A.a0, A.a1, un.x, uu.x),
+                                           rk_combine<R, FAST>(A.a0, A.a1, un.y, uu.y),
+                                           rk_combine<R, FAST>(A.a0, A.a1, un.z, uu.z),
+                                           rk_combine<R, FAST>(A.a0, A.a1, un.w, uu.w)};
                 }
             }
         }
@@ -562,9 +564,13 @@ __global__ void __launch_bounds__(kDiagThreads)
         // In the perturbation form e_lab is max(E, e_floor) - e_bg: the sums of
         // e_total and e_lab then miss N e_bg, which the host adds in FP64.
         const R e_lab = vmax(u.x, P.e_floor);
-        const V4<R> q = recover<R, false, MIXED>(u, P);
+        const V4<R> q = recover<R, false, MIXED>(u, P, phi);
         const R v2 = q.x * q.x + q.y * q.y + q.z * q.z;
-        const R e_total = R(0.5) * pi * pi + R(0.5) * grad2 + potential(phi, P) + e_lab;
+        // the thermal form's field holds V(phi, 0); the rest of V(phi, T) is in E
+        R pot;
+        if constexpr (MIXED == kThermal) pot = thermal_potential0(phi, P);
+        else pot = potential(phi, P);
+        const R e_total = R(0.5) * pi * pi + R(0.5) * grad2 + pot + e_lab;
         const R broken = phi > R(0.5) * P.phi_b ? R(1.0) : R(0.0);
         R kinetic;
         if constexpr (MIXED == kPert) kinetic = ((e_lab + q.w) + (P.e_bg + P.p_bg)) * v2;

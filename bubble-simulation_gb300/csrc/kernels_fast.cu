@@ -32,12 +32,14 @@ cudaError_t stage_v2_f32_fast(const StageArgs<float> &A, const LatticeParams<flo
     using namespace launch_detail;
     if (shape.tx != 32) return cudaErrorInvalidValue;
     if (shape.ty == 8) {
+        if (mode == dev::kThermal)
+            return stage_v2<float, true, dev::kThermal, 8>(A, P, shape.lz, maps, tma_ok, status, s);
         if (mode == dev::kGamma) return stage_v2<float, true, dev::kGamma, 8>(A, P, shape.lz, maps, tma_ok, status, s);
         if (mode == dev::kPert) return stage_v2<float, true, dev::kPert, 8>(A, P, shape.lz, maps, tma_ok, status, s);
         if (mode == dev::kMixed) return stage_v2<float, true, dev::kMixed, 8>(A, P, shape.lz, maps, tma_ok, status, s);
         return stage_v2<float, true, dev::kPlain, 8>(A, P, shape.lz, maps, tma_ok, status, s);
     }
-    if (shape.ty == 4 && mode != dev::kPert && mode != dev::kGamma) {
+    if (shape.ty == 4 && (mode == dev::kPlain || mode == dev::kMixed)) {
         if (mode == dev::kMixed) return stage_v2<float, true, dev::kMixed, 4>(A, P, shape.lz, maps, tma_ok, status, s);
         return stage_v2<float, true, dev::kPlain, 4>(A, P, shape.lz, maps, tma_ok, status, s);
     }

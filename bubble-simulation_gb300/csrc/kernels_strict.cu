@@ -35,6 +35,7 @@ cudaError_t stage_fused_f32_strict(const StageArgs<float> &A, const LatticeParam
 cudaError_t diag_f32(const V2<float> *field, const V4<float> *fluid,
                      const LatticeParams<float> &P, int mode, void *partials,
                      unsigned int *ticket, DiagResult *out, cudaStream_t s) {
+    if (mode == dev::kThermal) return diag<float, dev::kThermal>(field, fluid, P, partials, ticket, out, s);
     if (mode == dev::kGamma) return diag<float, dev::kGamma>(field, fluid, P, partials, ticket, out, s);
     if (mode == dev::kPert) return diag<float, dev::kPert>(field, fluid, P, partials, ticket, out, s);
     if (mode == dev::kMixed) return diag<float, dev::kMixed>(field, fluid, P, partials, ticket, out, s);
@@ -70,6 +71,8 @@ cudaError_t stage_v2_f32_strict(const StageArgs<float> &A, const LatticeParams<f
                                 int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
     using namespace launch_detail;
     if (shape.tx != 32 || shape.ty != 8) return cudaErrorInvalidValue;
+    if (mode == dev::kThermal)
+        return stage_v2<float, false, dev::kThermal, 8>(A, P, shape.lz, maps, tma_ok, status, s);
     if (mode == dev::kGamma) return stage_v2<float, false, dev::kGamma, 8>(A, P, shape.lz, maps, tma_ok, status, s);
     if (mode == dev::kPert) return stage_v2<float, false, dev::kPert, 8>(A, P, shape.lz, maps, tma_ok, status, s);
     if (mode == dev::kMixed) return stage_v2<float, false, dev::kMixed, 8>(A, P, shape.lz, maps, tma_ok, status, s);

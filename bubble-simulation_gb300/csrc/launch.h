@@ -37,7 +37,7 @@ cudaError_t stage_ref_f32(const StageArgs<float> &A, const V4<float> *prim,
 cudaError_t stage_fused_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P,
                                    TileShape shape, bool mixed, cudaStream_t s);
 // `mode`: 0 plain, 1 mixed, 2 perturbation form, 3 gamma-law equation of
-// state (physics.cuh kPlain/kMixed/kPert/kGamma).
+// state, 4 thermal potential (physics.cuh kPlain/kMixed/kPert/kGamma/kThermal).
 cudaError_t diag_f32(const V2<float> *field, const V4<float> *fluid,
                      const LatticeParams<float> &P, int mode, void *partials,
                      unsigned int *ticket, DiagResult *out, cudaStream_t s);

@@ -39,6 +39,11 @@ struct LatticeParams {
     // Gamma-law equation of state: c_s^2 = Gamma - 1 and the offset e0 of
     // e = p / (Gamma - 1) + e0; both 0 for the bag model.
     R eos_c2, eos_e0;
+    // Thermal potential V(phi) + gamma/2 (T^2 - T_ref^2) phi^2 - A/3 (T - T_ref) phi^3:
+    // th_k = a/3, th_g = gamma, th_h = A/3, th_a = A, th_lo = sqrt(3 gamma / (4 a))
+    // (the physical branch is T >= th_lo |phi|), th_i2a = 1/(2a), the radiation
+    // constant a and T_ref; all 0 for the other equations of state.
+    R th_k, th_g, th_h, th_a, th_lo, th_i2a, a_rad, t_ref;
 };
 
 // One SSP-RK3 stage: U_out = a0 U^n + a1 (U_in + dt L(U_in))

@@ -248,6 +248,24 @@ std::string validate_eos(const bubble_spec &spec) {
                 return "the gamma-law equation of state is built for BUBBLE_PRECISION_SINGLE";
             return {};
         }
+        case BUBBLE_EOS_THERMAL: {
+            // For T >= T_ref / sqrt(2) and |phi| <= phi_b: gamma <= a T_ref^2 /
+            // (6 phi_b^2) keeps the thermal mass term below half the radiation
+            // pressure (p >= a T^4 / 6 at A = 0) and the state on the branch
+            // T >= sqrt(3 gamma / (4a)) |phi|; A <= a T_ref^3 / (sqrt(2) phi_b^3)
+            // keeps p <= e (A phi^3 <= 2 a T^3), so |Z| <= E holds for every
+            // physical state and the regularisation never alters one
+            const float g = spec.eos_param[0], a_c = spec.eos_param[1];
+            const Derived d = derive(spec.model);
+            const float a = d.a_rad, t_ref = d.t_ref, pb = spec.model.phi_b;
+            const float g_max = a * t_ref * t_ref / (6.0f * pb * pb);
+            const float a_max = a * t_ref * t_ref * t_ref / (1.41421356f * pb * pb * pb);
+            if (!(g >= 0.0f && g <= g_max)) return "gamma must lie in [0, a T_ref^2 / (6 phi_b^2)]";
+            if (!(a_c >= 0.0f && a_c <= a_max)) return "A must lie in [0, a T_ref^3 / (sqrt(2) phi_b^3)]";
+            if (spec.precision != BUBBLE_PRECISION_SINGLE)
+                return "the thermal potential is built for BUBBLE_PRECISION_SINGLE";
+            return {};
+        }
         default:
             return "unknown equation of state";
     }

@@ -290,15 +290,149 @@ BUBBLE_DEV V4<R> prim_from_cons_gamma(const V4<R> &u, const LatticeParams<R> &P)
     return V4<R>{zx / d, zy / d, zz / d, p};
 }
 
+// ---------------------------------------------------------------------------
+//  Thermal potential (docs/EOS.md:120-150, shaders/potential.wgsl:29-37)
+// ---------------------------------------------------------------------------
+// V(phi, T) = V(phi) + gamma/2 (T^2 - T_ref^2) phi^2 - A/3 (T - T_ref) phi^3
+// equals the reference's V(phi) at T = T_ref, and is the finite-temperature
+// form gamma/2 (T^2 - T0^2) phi^2 - A/3 T phi^3 + lambda/4 phi^4 of the
+// reference's recipe when A = delta / T_ref and gamma T0^2 = gamma T_ref^2 - m2.
+// The field keeps the zero-temperature part V(phi, 0); the plasma carries
+// dV = gamma/2 T^2 phi^2 - A/3 T phi^3 in its free energy:
+//     p(T, phi) = a/3 T^4 - dV,   e = T dp/dT - p = a T^4 - gamma/2 T^2 phi^2,
+//     c_s^2 = (dp/dT) / (de/dT)   (at fixed phi),
+// and d(dV)/dphi passes between field and plasma the way the friction does
+// (dE += dV' pi, dZ -= dV' grad phi), so the conserved total is
+// 1/2 pi^2 + 1/2 |grad phi|^2 + V(phi, 0) + E.  On the physical branch
+// T >= th_lo |phi| (th_lo = sqrt(3 gamma / (4a))), e, de/dT and, for A >= 0
+// and phi >= 0, dp/dT are positive and p(T) is convex, so the inversions
+// below are fixed Newton counts with floors, like the gamma law's.
+constexpr int kThermalNewtonSteps = 8;
+
+template <typename R>
+BUBBLE_DEV R thermal_pressure(R T, R phi, const LatticeParams<R> &P) {
+    const R t2 = T * T, f2 = phi * phi;
+    return P.th_k * (t2 * t2) - (R(0.5) * P.th_g) * (t2 * f2) + P.th_h * (T * (f2 * phi));
+}
+template <typename R>
+BUBBLE_DEV R thermal_energy(R T, R phi, const LatticeParams<R> &P) {
+    const R t2 = T * T;
+    return P.a_rad * (t2 * t2) - (R(0.5) * P.th_g) * (t2 * (phi * phi));
+}
+// c_s^2 = (dp/dT) / (de/dT), held in [1e-4, 1] (an outer bound for HLL off the branch)
+template <typename R, bool FAST>
+BUBBLE_DEV R thermal_cs2(R T, R phi, const LatticeParams<R> &P) {
+    const R t2 = T * T, f2 = phi * phi;
+    const R dp = T * (R(4.0) * P.th_k * t2 - P.th_g * f2) + P.th_h * (f2 * phi);
+    const R de = vmax(T * (R(4.0) * P.a_rad * t2 - P.th_g * f2), R(1e-30));
+    R c2;
+    if constexpr (FAST) c2 = dp * rcp_approx(de);
+    else c2 = dp / de;
+    return vmin(vmax(c2, R(1e-4)), R(1.0));
+}
+// eos_temperature(p, phi): the root of p(T, phi) = p from the phi = 0 root,
+// each step held to [max(T_lo, T/2), 2T].
+template <typename R, bool FAST>
+BUBBLE_DEV R thermal_temperature(R p, R phi, const LatticeParams<R> &P) {
+    const R pp = vmax(p, P.p_floor);
+    const R lo = P.th_lo * fabs(phi);
+    const R f2 = phi * phi, h = P.th_h * (f2 * phi);
+    R T;
+    if constexpr (FAST) T = vmax(sqrt_approx(sqrt_approx(pp * rcp_approx(P.th_k))), lo);
+    else T = vmax(sqrt(sqrt(pp / P.th_k)), lo);
+#pragma unroll
+    for (int it = 0; it < kThermalNewtonSteps; ++it) {
+        const R t2 = T * T;
+        const R g = P.th_k * (t2 * t2) - (R(0.5) * P.th_g) * (t2 * f2) + P.th_h * (T * (f2 * phi)) - pp;
+        const R d = vmax(T * (R(4.0) * P.th_k * t2 - P.th_g * f2) + h, R(1e-30));
+        R tn;
+        if constexpr (FAST) tn = T - g * rcp_approx(d);
+        else tn = T - g / d;
+        T = vmin(vmax(tn, vmax(lo, R(0.5) * T)), R(2.0) * T);
+    }
+    return T;
+}
+// dV/dphi of the thermal potential at (phi, T) and its plasma part d(dV)/dphi
+template <typename R>
+BUBBLE_DEV R thermal_dpotential(R phi, R T, const LatticeParams<R> &P) {
+    return dpotential(phi, P) + phi * (P.th_g * (T * T - P.t_ref * P.t_ref) - P.th_a * ((T - P.t_ref) * phi));
+}
+template <typename R>
+BUBBLE_DEV R thermal_exchange(R phi, R T, const LatticeParams<R> &P) {
+    return phi * (P.th_g * (T * T) - P.th_a * (T * phi));
+}
+// V(phi, 0), the field's share of the potential (diagnostics)
+template <typename R>
+BUBBLE_DEV R thermal_potential0(R phi, const LatticeParams<R> &P) {
+    const R f2 = phi * phi;
+    return potential(phi, P) + f2 * (P.th_h * (P.t_ref * phi) - (R(0.5) * P.th_g) * (P.t_ref * P.t_ref));
+}
+// con2prim: f(p) = p - p(T(e), phi) = 0 with e = E - Z^2 / (E + p) and
+// T^2 = (gamma/2 phi^2 + sqrt((gamma/2 phi^2)^2 + 4 a e)) / (2a), the root of
+// e(T) = e on the branch; f' = 1 - c_s^2 Z^2 / (E + p)^2 > 0.
+template <typename R, bool FAST>
+BUBBLE_DEV V4<R> prim_from_cons_thermal(const V4<R> &u, R phi, const LatticeParams<R> &P) {
+    const R e_lab = vmax(u.x, P.e_floor);
+    R zx = u.y, zy = u.z, zz = u.w;
+    const R zcap = P.z_max * e_lab;
+    const R zlen = sqrt(zx * zx + zy * zy + zz * zz);
+    if (zlen > zcap) {
+        const R sc = zcap / vmax(zlen, R(1e-30));
+        zx = zx * sc;
+        zy = zy * sc;
+        zz = zz * sc;
+    }
+    const R z2 = zx * zx + zy * zy + zz * zz;
+    const R f2 = phi * phi;
+    const R g = (R(0.5) * P.th_g) * f2;
+    const R h = P.th_h * (f2 * phi);
+    const R a4 = R(4.0) * P.a_rad;
+    R X = (g + sqrt(g * g + a4 * e_lab)) * P.th_i2a;
+    R p = vmax(P.th_k * (X * X) - g * X + h * sqrt(X), P.p_floor);
+#pragma unroll
+    for (int it = 0; it < kThermalNewtonSteps; ++it) {
+        const R sp = e_lab + p;
+        R e, c2, r, d;
+        if constexpr (FAST) {
+            const R isp = rcp_approx(sp);
+            e = e_lab - z2 * isp;
+            X = (g + sqrt_approx(g * g + a4 * e)) * P.th_i2a;
+            const R T = sqrt_approx(X);
+            const R dp = T * (R(4.0) * P.th_k * X - P.th_g * f2) + h;
+            const R de = vmax(T * (a4 * X - P.th_g * f2), R(1e-30));
+            c2 = vmin(vmax(dp * rcp_approx(de), R(1e-4)), R(1.0));
+            r = p - (P.th_k * (X * X) - g * X + h * T);
+            d = R(1.0) - c2 * z2 * (isp * isp);
+            p = vmax(p - r * rcp_approx(d), P.p_floor);
+        } else {
+            e = e_lab - z2 / sp;
+            X = (g + sqrt(g * g + a4 * e)) * P.th_i2a;
+            const R T = sqrt(X);
+            const R dp = T * (R(4.0) * P.th_k * X - P.th_g * f2) + h;
+            const R de = vmax(T * (a4 * X - P.th_g * f2), R(1e-30));
+            c2 = vmin(vmax(dp / de, R(1e-4)), R(1.0));
+            r = p - (P.th_k * (X * X) - g * X + h * T);
+            d = R(1.0) - c2 * z2 / (sp * sp);
+            p = vmax(p - r / d, P.p_floor);
+        }
+    }
+    const R dd = vmax(e_lab + p, R(1e-30));
+    return V4<R>{zx / dd, zy / dd, zz / dd, p};
+}
+
 // Forms of a lattice (the FORM parameter of the kernels): the bag model in
 // plain FP32; mixed = FP64 primitive recovery where the Lorentz factor
 // exceeds 3; perturbation = mixed, with E stored as E - e_bg; gamma = the
-// gamma-law equation of state in plain arithmetic.
-constexpr int kPlain = 0, kMixed = 1, kPert = 2, kGamma = 3;
+// gamma-law equation of state in plain arithmetic; thermal = the thermal
+// potential's plasma in plain arithmetic (its EOS depends on phi).
+constexpr int kPlain = 0, kMixed = 1, kPert = 2, kGamma = 3, kThermal = 4;
 
+// `phi` is the cell's field value; only the thermal form's EOS reads it.
 template <typename R, bool FAST, int MODE>
-BUBBLE_DEV V4<R> recover(const V4<R> &u, const LatticeParams<R> &P) {
-    if constexpr (MODE == kGamma) {
+BUBBLE_DEV V4<R> recover(const V4<R> &u, const LatticeParams<R> &P, R phi = R(0)) {
+    if constexpr (MODE == kThermal) {
+        return prim_from_cons_thermal<R, FAST>(u, phi, P);
+    } else if constexpr (MODE == kGamma) {
         return prim_from_cons_gamma<R, FAST>(u, P);
     } else if constexpr (MODE == kPert) {
         V4<R> q = prim_from_cons_pert<R, FAST>(u, P);
@@ -406,21 +540,31 @@ struct FaceSide {
 // constant p_bg would cancel in every flux difference.
 // GAMMA (FORM kGamma): w = p / c2 + p + e0 and the general wave speeds
 // with c_s^2 = c2; E = w W^2 - p and the fluxes as for the bag model.
+// THERMAL (FORM kThermal): w = e(T, phi) + p with T = eos_temperature(p, phi)
+// and c_s^2(T, phi), phi the field value of the state's own cell.
 template <int AXIS, typename R, bool FAST, int FORM = kPlain>
-BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2, const LatticeParams<R> &P) {
+BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2, const LatticeParams<R> &P, R phi = R(0)) {
     constexpr bool PERT = FORM == kPert;
     FaceSide<R> s;
     const R vx = q.x, vy = q.y, vz = q.z, p = q.w;
-    if constexpr (FORM == kGamma) {
+    if constexpr (FORM == kGamma || FORM == kThermal) {
         const R vd = comp<AXIS>(q);
         const R v2 = vmin(vx * vx + vy * vy + vz * vz, zmax2);
-        const R cs2 = P.eos_c2;
+        R cs2, enth;
+        if constexpr (FORM == kThermal) {
+            const R T = thermal_temperature<R, FAST>(p, phi, P);
+            enth = thermal_energy(T, phi, P) + p;
+            cs2 = thermal_cs2<R, FAST>(T, phi, P);
+        } else {
+            enth = gamma_enthalpy(p, P);
+            cs2 = P.eos_c2;
+        }
         R w, den_inv;
         if constexpr (FAST) {
-            w = gamma_enthalpy(p, P) * rcp_approx(R(1.0) - v2);
+            w = enth * rcp_approx(R(1.0) - v2);
             den_inv = rcp_approx(R(1.0) - v2 * cs2);
         } else {
-            w = gamma_enthalpy(p, P) / (R(1.0) - v2);
+            w = enth / (R(1.0) - v2);
         }
         s.u = V4<R>{w - p, w * vx, w * vy, w * vz};
         const R cs = sqrt(cs2);
@@ -488,12 +632,13 @@ BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2, const LatticeParams<R>
     return s;
 }
 
-// hll_flux(q_l, q_r, axis).  The phi arguments of the reference's hll_flux
-// reach only the bag EOS functions, which ignore them, so they are dropped.
+// hll_flux(q_l, phi_l, q_r, phi_r, axis).  The phi arguments reach only the
+// EOS functions; the forms whose EOS ignores phi pass 0.
 template <int AXIS, typename R, bool FAST, int FORM = kPlain>
-BUBBLE_DEV V4<R> hll_flux(const V4<R> &ql, const V4<R> &qr, R zmax2, const LatticeParams<R> &P) {
-    const FaceSide<R> L = face_side<AXIS, R, FAST, FORM>(ql, zmax2, P);
-    const FaceSide<R> Rt = face_side<AXIS, R, FAST, FORM>(qr, zmax2, P);
+BUBBLE_DEV V4<R> hll_flux(const V4<R> &ql, const V4<R> &qr, R zmax2, const LatticeParams<R> &P, R phi_l = R(0),
+                          R phi_r = R(0)) {
+    const FaceSide<R> L = face_side<AXIS, R, FAST, FORM>(ql, zmax2, P, phi_l);
+    const FaceSide<R> Rt = face_side<AXIS, R, FAST, FORM>(qr, zmax2, P, phi_r);
     const R s_min = vmin(vmin(L.lm, Rt.lm), R(0.0));
     const R s_max = vmax(vmax(L.lp, Rt.lp), R(0.0));
     const R den = vmax(s_max - s_min, R(1e-12));
@@ -511,6 +656,23 @@ BUBBLE_DEV V4<R> hll_flux(const V4<R> &ql, const V4<R> &qr, R zmax2, const Latti
                      (s_max * L.f.z - s_min * Rt.f.z + smm * (Rt.u.z - L.u.z)) / den,
                      (s_max * L.f.w - s_min * Rt.f.w + smm * (Rt.u.w - L.u.w)) / den};
     }
+}
+
+// ---------------------------------------------------------------------------
+//  SSP-RK3 stage combine a0 U^n + a1 U1 (shaders/step.wgsl:170-173)
+// ---------------------------------------------------------------------------
+// In binary32 fl(1/3) + fl(2/3) = 1 + 2^-25, so the reference's form is that
+// much too large before rounding on the third stage; over evolving cells the
+// rounding is unbiased and the mean keeps the excess: a systematic energy
+// drift of about 3e-8 per step that the FP64 scheme does not have (measured:
+// 3.2e-5 of excess drift over 1300 steps at 128^3, 7e-5 over 2900 at 256^3).  The
+// fast arithmetic evaluates U^n + a1 (U1 - U^n), whose weights sum to 1
+// exactly; the strict arithmetic keeps the reference's expression, for bit
+// parity with the oracle.
+template <typename R, bool FAST>
+BUBBLE_DEV R rk_combine(R a0, R a1, R un, R u1) {
+    if constexpr (FAST) return un + a1 * (u1 - un);
+    else return a0 * un + a1 * u1;
 }
 
 // ---------------------------------------------------------------------------

@@ -24,7 +24,10 @@ cudaError_t vis_f32(const V2<float> *field, const V4<float> *fluid, const Lattic
                     float t_ref, float dof_ratio, int mode, cudaSurfaceObject_t surf, cudaStream_t s) {
     const uint64_t n = (uint64_t)P.nx * P.ny * P.nz;
     const dev::VisConsts<float> C{a_rad, t_ref, dof_ratio};
-    if (mode == dev::kGamma) dev::vis_kernel<float, dev::kGamma><<<vis_grid(n), 256, 0, s>>>(field, fluid, P, C, surf);
+    if (mode == dev::kThermal)
+        dev::vis_kernel<float, dev::kThermal><<<vis_grid(n), 256, 0, s>>>(field, fluid, P, C, surf);
+    else if (mode == dev::kGamma)
+        dev::vis_kernel<float, dev::kGamma><<<vis_grid(n), 256, 0, s>>>(field, fluid, P, C, surf);
     else if (mode == dev::kPert) dev::vis_kernel<float, dev::kPert><<<vis_grid(n), 256, 0, s>>>(field, fluid, P, C, surf);
     else if (mode == dev::kMixed) dev::vis_kernel<float, dev::kMixed><<<vis_grid(n), 256, 0, s>>>(field, fluid, P, C, surf);
     else dev::vis_kernel<float, dev::kPlain><<<vis_grid(n), 256, 0, s>>>(field, fluid, P, C, surf);

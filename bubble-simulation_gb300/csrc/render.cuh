@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(256) vis_kernel(const V2<R> *__restrict__ fiel
         const int z = (int)(yz / (uint64_t)P.ny);
         const R phi = field[i].x;
         const V4<R> u = fluid[i];
-        const V4<R> q = recover<R, false, MIXED>(u, P);
+        const V4<R> q = recover<R, false, MIXED>(u, P, phi);
         // the full p and max(E, e_floor); the perturbation form adds its backgrounds
         const R p = MIXED == kPert ? P.p_bg + q.w : q.w;
         const R e_lab = MIXED == kPert ? P.e_bg + vmax(u.x, P.e_floor) : vmax(u.x, P.e_floor);
@@ -64,7 +64,9 @@ __global__ void __launch_bounds__(256) vis_kernel(const V2<R> *__restrict__ fiel
             const R smooth = h * h * (R(3.0) - R(2.0) * h);
             a = C.a_rad * (R(1.0) + (C.dof_ratio - R(1.0)) * smooth);
         }
-        const R temp = sqrt(sqrt(R(3.0) * pt / a));
+        R temp;
+        if constexpr (MIXED == kThermal) temp = thermal_temperature<R, false>(pt, phi, P);
+        else temp = sqrt(sqrt(R(3.0) * pt / a));
         const R kinetic = (e_lab + p) * v2;
         ushort4 t;
         t.x = half_bits((float)(phi / P.phi_b));

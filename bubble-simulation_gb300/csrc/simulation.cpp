@@ -215,6 +215,17 @@ LatticeParams<float> Simulation::params_f32() const {
         p.eos_c2 = spec_.eos_param[0] - 1.0f;
         p.eos_e0 = spec_.eos_param[1];
     }
+    if (spec_.eos == BUBBLE_EOS_THERMAL) {
+        const float g = spec_.eos_param[0], a = spec_.eos_param[1];
+        p.th_k = h.a_rad / 3.0f;
+        p.th_g = g;
+        p.th_h = a / 3.0f;
+        p.th_a = a;
+        p.th_lo = std::sqrt(3.0f * g / (4.0f * h.a_rad));
+        p.th_i2a = 1.0f / (2.0f * h.a_rad);
+        p.a_rad = h.a_rad;
+        p.t_ref = h.t_ref;
+    }
     if (spec_.precision == BUBBLE_PRECISION_PERTURBATION) {
         // the stored energy is E - e_bg and the primitive pressure p - p_bg;
         // the floors move with them
@@ -228,6 +239,7 @@ LatticeParams<float> Simulation::params_f32() const {
 
 int Simulation::arith_mode() const {
     if (spec_.eos == BUBBLE_EOS_GAMMA_LAW) return 3;
+    if (spec_.eos == BUBBLE_EOS_THERMAL) return 4;
     switch (spec_.precision) {
         case BUBBLE_PRECISION_MIXED: return 1;
         case BUBBLE_PRECISION_PERTURBATION: return 2;
@@ -322,7 +334,8 @@ int Simulation::resize(const uint32_t grid[3], std::string &err) {
 
 int Simulation::set_tile(TileShape t, std::string &err) {
     const bool strict = !is_f64() && spec_.math == BUBBLE_MATH_STRICT;
-    const bool pert = spec_.precision == BUBBLE_PRECISION_PERTURBATION || spec_.eos == BUBBLE_EOS_GAMMA_LAW;
+    const bool pert = spec_.precision == BUBBLE_PRECISION_PERTURBATION || spec_.eos == BUBBLE_EOS_GAMMA_LAW ||
+                      spec_.eos == BUBBLE_EOS_THERMAL;
     // the synchronous-staging and strict kernels are built for fewer shapes
     // than the default one; their launches check the shape themselves
     if (t.tx != 32 || !launch::v2_shape_supported(is_f64(), t.ty) || ((strict || pert) && t.ty != 8) || t.lz < 1) {
@@ -397,8 +410,8 @@ int Simulation::stage_launch(int stage, uint32_t in_slot, uint32_t out_slot, std
     const bool mixed = spec_.precision == BUBBLE_PRECISION_MIXED;
     const int mode = arith_mode();
     if (mode >= 2 && path_ != KernelPath::Fused) {
-        err = "the perturbation form and the gamma-law equation of state run on the default (fused, "
-              "asynchronous staging) kernel path only";
+        err = "the perturbation form and the gamma-law and thermal equations of state run on the default "
+              "(fused, asynchronous staging) kernel path only";
         return BUBBLE_ERR_INVALID;
     }
     if (is_f64()) {

@@ -265,8 +265,9 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
             const int gy = wrap1(y0 - 2 + j, P.ny);
             const size_t g = base + (size_t)gy * P.nx + gx;
             const V4<R> u = A.fluid_in[g];
-            ph[j * PW + i] = A.field_in[g].x;
-            pr[j * PW + i] = sanitise(recover<R, FAST, MIXED>(u, P), P.p_floor, zmax2);
+            const R phv = A.field_in[g].x;
+            ph[j * PW + i] = phv;
+            pr[j * PW + i] = sanitise(recover<R, FAST, MIXED>(u, P, phv), P.p_floor, zmax2);
         }
     };
     auto z_states = [&](int p, int n, V4<R> &lo, V4<R> &hi) {
@@ -285,7 +286,13 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
         z_states(z0 - 1, n, lo_m, hi_m);
         z_states(z0, n, lo_0, hi_0);
         zhi[((z0 + 8) & 1) * NC + n] = hi_0;
-        fzs[((z0 - 1 + 8) & 1) * NC + n] = hll_flux<2, R, FAST, MIXED>(hi_m, lo_0, zmax2, P);
+        R phl = R(0), phr = R(0);
+        if constexpr (MIXED == kThermal) {
+            const int c = (n / TX + 2) * PW + (n % TX + 2);
+            phl = phi_slot(z0 - 1)[c];
+            phr = phi_slot(z0)[c];
+        }
+        fzs[((z0 - 1 + 8) & 1) * NC + n] = hll_flux<2, R, FAST, MIXED>(hi_m, lo_0, zmax2, P, phl, phr);
     }
     __syncthreads();
     stage_plane_sync(z0 + 2);
@@ -330,6 +337,7 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
         const V4<R> *pr_zm1 = prim_slot(z - 1), *pr_z = prim_slot(z);
         const V4<R> *pr_zp1 = prim_slot(z + 1), *pr_zp2 = prim_slot(z + 2);
         const R *ph_zm2 = phi_slot(z - 2), *ph_zm1 = phi_slot(z - 1), *ph_z = phi_slot(z);
+        const R *ph_zp1 = phi_slot(z + 1);
         V4<R> *fz_rd_m = fzs + ((z - 2 + 8) & 1) * NC;   // face below plane z-1
         V4<R> *fz_rd_p = fzs + ((z - 1 + 8) & 1) * NC;   // face above plane z-1
         V4<R> *zhi_next = zhi + ((z + 1 + 8) & 1) * NC;
@@ -392,11 +400,21 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
                     if constexpr (FAST) gam = rsqrt_approx(vmax(R(1.0) - vv, R(1e-12)));
                     else gam = R(1.0) / sqrt(vmax(R(1.0) - vv, R(1e-12)));
                     const R drag = P.eta * (gam * (pi0 + (q0.x * gx + q0.y * gy + q0.z * gz)));
-                    const R d_pi = laplacian - dpotential(phi0, P) - drag;
-                    const R dE = -fd.x + drag * pi0;
-                    const R dZx = -fd.y - drag * gx;
-                    const R dZy = -fd.z - drag * gy;
-                    const R dZz = -fd.w - drag * gz;
+                    // the thermal potential's dV/dphi at the cell's temperature, and
+                    // its plasma part, exchanged like the friction
+                    R dpot, src = drag;
+                    if constexpr (MIXED == kThermal) {
+                        const R T0 = thermal_temperature<R, FAST>(q0.w, phi0, P);
+                        dpot = thermal_dpotential(phi0, T0, P);
+                        src = drag + thermal_exchange(phi0, T0, P);
+                    } else {
+                        dpot = dpotential(phi0, P);
+                    }
+                    const R d_pi = laplacian - dpot - drag;
+                    const R dE = -fd.x + src * pi0;
+                    const R dZx = -fd.y - src * gx;
+                    const R dZy = -fd.z - src * gy;
+                    const R dZz = -fd.w - src * gz;
                     const V2<R> fu{pf.x + A.dt * pi0, pf.y + A.dt * d_pi};
                     const V4<R> uu{pu.x + A.dt * dE, pu.y + A.dt * dZx, pu.z + A.dt * dZy, pu.w + A.dt * dZz};
                     const size_t g = (size_t)zc * plane + c_off;
@@ -404,9 +422,12 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
                         A.field_out[g] = V2<R>{A.a1 * fu.x, A.a1 * fu.y};
                         A.fluid_out[g] = V4<R>{A.a1 * uu.x, A.a1 * uu.y, A.a1 * uu.z, A.a1 * uu.w};
                     } else {
-                        A.field_out[g] = V2<R>{A.a0 * pfn.x + A.a1 * fu.x, A.a0 * pfn.y + A.a1 * fu.y};
-                        A.fluid_out[g] = V4<R>{A.a0 * pun.x + A.a1 * uu.x, A.a0 * pun.y + A.a1 * uu.y,
-                                               A.a0 * pun.z + A.a1 * uu.z, A.a0 * pun.w + A.a1 * uu.w};
+                        A.field_out[g] = V2<R>{rk_combine<R, FAST>(A.a0, A.a1, pfn.x, fu.x),
+                                               rk_combine<R, FAST>(A.a0, A.a1, pfn.y, fu.y)};
+                        A.fluid_out[g] = V4<R>{rk_combine<R, FAST>(A.a0, A.a1, pun.x, uu.x),
+                                               rk_combine<R, FAST>(A.a0, A.a1, pun.y, uu.y),
+                                               rk_combine<R, FAST>(A.a0, A.a1, pun.z, uu.z),
+                                               rk_combine<R, FAST>(A.a0, A.a1, pun.w, uu.w)};
                     }
                     return;
                 }
@@ -485,15 +506,22 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
                     const int c = ya_c[r];
                     if (!do_a || c < 0) return;
                     const V4<R> u = raw_ua[c];
-                    ph_a[c] = raw_fa[c].x;
-                    pr_a[c] = sanitise(recover<R, FAST, MIXED>(u, P), P.p_floor, zmax2);
+                    const R phv = raw_fa[c].x;
+                    ph_a[c] = phv;
+                    pr_a[c] = sanitise(recover<R, FAST, MIXED>(u, P, phv), P.p_floor, zmax2);
                     return;
                 }
             }
             if constexpr (lo < L::Y_A + L::Y_Z && hi > L::Y_A) {
                 if (k < L::Y_A + L::Y_Z) {
                     const int kk = k - L::Y_A;
-                    fz_wr[kk] = hll_flux<2, R, FAST, MIXED>(zhi_cur[kk], zlo[kk], zmax2, P);
+                    R phl = R(0), phr = R(0);
+                    if constexpr (MIXED == kThermal) {
+                        const int c = (kk / TX + 2) * PW + (kk % TX + 2);
+                        phl = ph_z[c];
+                        phr = ph_zp1[c];
+                    }
+                    fz_wr[kk] = hll_flux<2, R, FAST, MIXED>(zhi_cur[kk], zlo[kk], zmax2, P, phl, phr);
                     return;
                 }
             }
@@ -501,7 +529,14 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
                 if (k < L::Y_A + L::Y_Z + L::Y_Y) {
                     // face between rows f-1 and f: yhi[f*TX+i] = yhi[q], ylo[(f+1)*TX+i] = ylo[q+TX]
                     const int q = k - L::Y_A - L::Y_Z;
-                    fys[q] = hll_flux<1, R, FAST, MIXED>(yhi[q], ylo[q + TX], zmax2, P);
+                    R phl = R(0), phr = R(0);
+                    if constexpr (MIXED == kThermal) {
+                        // states of smem cells (f+1, i+2) and (f+2, i+2), f = q / TX
+                        const int c = (q / TX + 1) * PW + (q % TX + 2);
+                        phl = ph_z[c];
+                        phr = ph_z[c + PW];
+                    }
+                    fys[q] = hll_flux<1, R, FAST, MIXED>(yhi[q], ylo[q + TX], zmax2, P, phl, phr);
                     return;
                 }
             }
@@ -510,7 +545,14 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
                     // face between columns f-1 and f of row j: states j*(TX+2)+f and +1
                     const int q = k - L::Y_A - L::Y_Z - L::Y_Y;
                     const int j = q / (TX + 1);
-                    fxs[q] = hll_flux<0, R, FAST, MIXED>(xhi[q + j], xlo[q + j + 1], zmax2, P);
+                    R phl = R(0), phr = R(0);
+                    if constexpr (MIXED == kThermal) {
+                        // states of smem cells (j+2, f+1) and (j+2, f+2), f = q - j (TX+1)
+                        const int c = (j + 2) * PW + (q - j * (TX + 1) + 1);
+                        phl = ph_z[c];
+                        phr = ph_z[c + 1];
+                    }
+                    fxs[q] = hll_flux<0, R, FAST, MIXED>(xhi[q + j], xlo[q + j + 1], zmax2, P, phl, phr);
                 }
             }
         });

@@ -141,6 +141,14 @@ int bubble_make_schedule(int32_t mode, uint64_t count, float radius,
 #define BUBBLE_EOS_GAMMA_LAW 2 /* e = p/(Gamma - 1) + e0, c_s^2 = Gamma - 1, Newton
                                   inversion (docs/EOS.md:86-118); Gamma = eos_param[0]
                                   in (1, 2], e0 = eos_param[1] in [0, e_ref)          */
+#define BUBBLE_EOS_THERMAL 3   /* temperature-dependent potential (docs/EOS.md:120-150):
+                                  V(phi, T) = V(phi) + gamma/2 (T^2 - T_ref^2) phi^2
+                                  - A/3 (T - T_ref) phi^3, the plasma carrying the
+                                  T-dependent part, p = a T^4/3 - that part; gamma =
+                                  eos_param[0] in [0, a T_ref^2 / (6 phi_b^2)], A =
+                                  eos_param[1] in [0, a T_ref^3 / (sqrt(2) phi_b^3)]
+                                  (p <= e); A = delta / T_ref would be the recipe's
+                                  -A T phi^3 / 3 form; FP32 only                     */
 
 typedef struct bubble_spec {
     bubble_model model;

@@ -216,8 +216,92 @@ inline vec4<R> eos_prim_from_cons_gamma(const SimParams<R> &P, vec4<R> u_raw) {
     return {u.y / d, u.z / d, u.w / d, p};
 }
 
-template <typename R, bool PERT = false, bool GAMMA = false>
+// Thermal potential (docs/EOS.md:120-150): V(phi, T) = V(phi)
+// + gamma/2 (T^2 - T_ref^2) phi^2 - A/3 (T - T_ref) phi^3, the field keeping
+// V(phi, 0) and the plasma dV = gamma/2 T^2 phi^2 - A/3 T phi^3:
+// p = a/3 T^4 - dV, e = a T^4 - gamma/2 T^2 phi^2, c_s^2 = (dp/dT)/(de/dT).
+// Constants as the library's host rounds them (oracle_set_thermal):
+// k = a/3, gamma, h = A/3, A, lo = sqrt(3 gamma / (4a)), i2a = 1/(2a).
+float g_th_k = 0.0f, g_th_g = 0.0f, g_th_h = 0.0f, g_th_a = 0.0f, g_th_lo = 0.0f, g_th_i2a = 0.0f;
+
+template <typename R>
+inline R thermal_energy(const SimParams<R> &P, R T, R phi) {
+    const R t2 = T * T;
+    return P.a_rad * (t2 * t2) - (R(0.5) * R(g_th_g)) * (t2 * (phi * phi));
+}
+// c_s^2 held in [1e-4, 1]
+template <typename R>
+inline R thermal_cs2(const SimParams<R> &P, R T, R phi) {
+    const R t2 = T * T, f2 = phi * phi;
+    const R dp = T * (R(4.0) * R(g_th_k) * t2 - R(g_th_g) * f2) + R(g_th_h) * (f2 * phi);
+    const R de = wmax(T * (R(4.0) * P.a_rad * t2 - R(g_th_g) * f2), R(1e-30));
+    return wmin(wmax(dp / de, R(1e-4)), R(1.0));
+}
+// eos_temperature(p, phi): eight Newton steps on p(T, phi) = p from the
+// phi = 0 root, each held to [max(lo |phi|, T/2), 2T].
+template <typename R>
+inline R thermal_temperature(const SimParams<R> &P, R p, R phi) {
+    const R k = R(g_th_k), gm = R(g_th_g), hc = R(g_th_h);
+    const R pp = wmax(p, P.p_floor);
+    const R lo = R(g_th_lo) * std::fabs(phi);
+    const R f2 = phi * phi, h = hc * (f2 * phi);
+    R T = wmax(std::sqrt(std::sqrt(pp / k)), lo);
+    for (int it = 0; it < 8; ++it) {
+        const R t2 = T * T;
+        const R g = k * (t2 * t2) - (R(0.5) * gm) * (t2 * f2) + hc * (T * (f2 * phi)) - pp;
+        const R d = wmax(T * (R(4.0) * k * t2 - gm * f2) + h, R(1e-30));
+        const R tn = T - g / d;
+        T = wmin(wmax(tn, wmax(lo, R(0.5) * T)), R(2.0) * T);
+    }
+    return T;
+}
+template <typename R>
+inline R thermal_dpotential(const SimParams<R> &P, R phi, R T) {
+    return dpotential(P, phi) +
+           phi * (R(g_th_g) * (T * T - P.t_ref * P.t_ref) - R(g_th_a) * ((T - P.t_ref) * phi));
+}
+template <typename R>
+inline R thermal_exchange(R phi, R T) {
+    return phi * (R(g_th_g) * (T * T) - R(g_th_a) * (T * phi));
+}
+template <typename R>
+inline R thermal_potential0(const SimParams<R> &P, R phi) {
+    const R f2 = phi * phi;
+    return potential(P, phi) + f2 * (R(g_th_h) * (P.t_ref * phi) - (R(0.5) * R(g_th_g)) * (P.t_ref * P.t_ref));
+}
+// Inversion: f(p) = p - p(T(e), phi), e = E - Z^2 / (E + p), T^2 the root of
+// e(T) = e on the physical branch; eight Newton steps floored at p_floor.
+template <typename R>
+inline vec4<R> eos_prim_from_cons_thermal(const SimParams<R> &P, vec4<R> u_raw, R phi) {
+    const vec4<R> u = eos_regularise(P, u_raw);
+    const R e_lab = u.x;
+    const R z2 = u.y * u.y + u.z * u.z + u.w * u.w;
+    const R k = R(g_th_k), gm = R(g_th_g), i2a = R(g_th_i2a);
+    const R f2 = phi * phi;
+    const R g = (R(0.5) * gm) * f2;
+    const R h = R(g_th_h) * (f2 * phi);
+    const R a4 = R(4.0) * P.a_rad;
+    R X = (g + std::sqrt(g * g + a4 * e_lab)) * i2a;
+    R p = wmax(k * (X * X) - g * X + h * std::sqrt(X), P.p_floor);
+    for (int it = 0; it < 8; ++it) {
+        const R sp = e_lab + p;
+        const R e = e_lab - z2 / sp;
+        X = (g + std::sqrt(g * g + a4 * e)) * i2a;
+        const R T = std::sqrt(X);
+        const R dp = T * (R(4.0) * k * X - gm * f2) + h;
+        const R de = wmax(T * (a4 * X - gm * f2), R(1e-30));
+        const R c2 = wmin(wmax(dp / de, R(1e-4)), R(1.0));
+        const R r = p - (k * (X * X) - g * X + h * T);
+        const R d = R(1.0) - c2 * z2 / (sp * sp);
+        p = wmax(p - r / d, P.p_floor);
+    }
+    const R d = wmax(e_lab + p, R(1e-30));
+    return {u.y / d, u.z / d, u.w / d, p};
+}
+
+template <typename R, bool PERT = false, bool GAMMA = false, bool THERMAL = false>
 inline vec4<R> eos_prim_from_cons(const SimParams<R> &P, vec4<R> u_raw, R phi) {
+    if (THERMAL) return eos_prim_from_cons_thermal(P, u_raw, phi);
     if (GAMMA) return eos_prim_from_cons_gamma(P, u_raw);
     if (PERT) return eos_prim_from_cons_pert(P, u_raw);
     const vec4<R> u = eos_regularise(P, u_raw);
@@ -229,13 +313,16 @@ inline vec4<R> eos_prim_from_cons(const SimParams<R> &P, vec4<R> u_raw, R phi) {
 }
 // PERT: the energy component is E - e_bg = w W^2 v^2 + 3 (p - p_bg); `w_out`
 // returns w W^2 for the energy flux w W^2 v_d.
-template <typename R, bool PERT = false, bool GAMMA = false>
+template <typename R, bool PERT = false, bool GAMMA = false, bool THERMAL = false>
 inline vec4<R> eos_cons_from_prim(const SimParams<R> &P, vec4<R> q, R phi, R *w_out = nullptr) {
     const R p = q.w;
     const R v2 = wmin(q.x * q.x + q.y * q.y + q.z * q.z, P.z_max * P.z_max);
     const R pf = PERT ? P.e_ref / R(3.0) + p : p;
-    // gamma law: w = e + p = p / c2 + p + e0
-    const R w_gam2 = (GAMMA ? p / R(g_eos_c2) + p + R(g_eos_e0) : eos_enthalpy_from_pressure(pf, phi)) / (R(1.0) - v2);
+    // gamma law: w = e + p = p / c2 + p + e0; thermal: e(T(p, phi), phi) + p
+    R enth;
+    if (THERMAL) enth = thermal_energy(P, thermal_temperature(P, p, phi), phi) + p;
+    else enth = GAMMA ? p / R(g_eos_c2) + p + R(g_eos_e0) : eos_enthalpy_from_pressure(pf, phi);
+    const R w_gam2 = enth / (R(1.0) - v2);
     if (w_out) *w_out = w_gam2;
     if (PERT) return {w_gam2 * v2 + R(3.0) * p, w_gam2 * q.x, w_gam2 * q.y, w_gam2 * q.z};
     return {w_gam2 - p, w_gam2 * q.x, w_gam2 * q.y, w_gam2 * q.z};
@@ -256,11 +343,12 @@ inline vec4<R> eos_flux(vec4<R> q, vec4<R> u, int axis, R w = R(0)) {
     if (axis == 2) f.w = f.w + p;
     return f;
 }
-template <typename R, bool GAMMA = false>
+template <typename R, bool GAMMA = false, bool THERMAL = false>
 inline void eos_wave_speeds(const SimParams<R> &P, vec4<R> q, R phi, int axis, R &lm, R &lp) {
     const R v2 = wmin(q.x * q.x + q.y * q.y + q.z * q.z, P.z_max * P.z_max);
     const R vd = axis_comp(q, axis);
-    const R cs2 = GAMMA ? R(g_eos_c2) : eos_sound_speed2(q.w, phi);
+    const R cs2 = THERMAL ? thermal_cs2(P, thermal_temperature(P, q.w, phi), phi)
+                          : (GAMMA ? R(g_eos_c2) : eos_sound_speed2(q.w, phi));
     const R cs = std::sqrt(cs2);
     const R denom = R(1.0) - v2 * cs2;
     const R rad = wmax((R(1.0) - v2) * (R(1.0) - vd * vd - cs2 * (v2 - vd * vd)), R(0.0));
@@ -288,16 +376,16 @@ inline vec4<R> sanitise(const SimParams<R> &P, vec4<R> q) {
     return {vx, vy, vz, p};
 }
 
-template <typename R, bool PERT = false, bool GAMMA = false>
+template <typename R, bool PERT = false, bool GAMMA = false, bool THERMAL = false>
 inline vec4<R> hll_flux(const SimParams<R> &P, vec4<R> q_l, R phi_l, vec4<R> q_r, R phi_r, int axis) {
     R w_l, w_r;
-    const vec4<R> u_l = eos_cons_from_prim<R, PERT, GAMMA>(P, q_l, phi_l, &w_l);
-    const vec4<R> u_r = eos_cons_from_prim<R, PERT, GAMMA>(P, q_r, phi_r, &w_r);
+    const vec4<R> u_l = eos_cons_from_prim<R, PERT, GAMMA, THERMAL>(P, q_l, phi_l, &w_l);
+    const vec4<R> u_r = eos_cons_from_prim<R, PERT, GAMMA, THERMAL>(P, q_r, phi_r, &w_r);
     const vec4<R> f_l = eos_flux<R, PERT>(q_l, u_l, axis, w_l);
     const vec4<R> f_r = eos_flux<R, PERT>(q_r, u_r, axis, w_r);
     R lml, lpl, lmr, lpr;
-    eos_wave_speeds<R, GAMMA>(P, q_l, phi_l, axis, lml, lpl);
-    eos_wave_speeds<R, GAMMA>(P, q_r, phi_r, axis, lmr, lpr);
+    eos_wave_speeds<R, GAMMA, THERMAL>(P, q_l, phi_l, axis, lml, lpl);
+    eos_wave_speeds<R, GAMMA, THERMAL>(P, q_r, phi_r, axis, lmr, lpr);
     const R s_min = wmin(wmin(lml, lmr), R(0.0));
     const R s_max = wmax(wmax(lpl, lpr), R(0.0));
     const R den = wmax(s_max - s_min, R(1e-12));
@@ -327,7 +415,7 @@ inline vec4<R> ld4(const R *a, size_t i) {
 }
 
 // step.wgsl main for one cell.
-template <typename R, bool PERT = false, bool GAMMA = false>
+template <typename R, bool PERT = false, bool GAMMA = false, bool THERMAL = false>
 void step_cell(const SimParams<R> &P, const StageParams<R> &S, const R *field_n, const R *fluid_n,
                const R *field_in, const R *fluid_in, const R *prim, R *field_out, R *fluid_out,
                int cx, int cy, int cz) {
@@ -355,9 +443,9 @@ void step_cell(const SimParams<R> &P, const StageParams<R> &S, const R *field_n,
         const vec4<R> slope_m1 = limit_slope4(sub(qm1, qm2), sub(q0, qm1));
         const vec4<R> slope_0 = limit_slope4(sub(q0, qm1), sub(qp1, q0));
         const vec4<R> slope_p1 = limit_slope4(sub(qp1, q0), sub(qp2, qp1));
-        const vec4<R> f_minus = hll_flux<R, PERT, GAMMA>(P, sanitise(P, add(qm1, scale(R(0.5), slope_m1))), phi_m,
+        const vec4<R> f_minus = hll_flux<R, PERT, GAMMA, THERMAL>(P, sanitise(P, add(qm1, scale(R(0.5), slope_m1))), phi_m,
                                          sanitise(P, sub(q0, scale(R(0.5), slope_0))), phi0, axis);
-        const vec4<R> f_plus = hll_flux<R, PERT, GAMMA>(P, sanitise(P, add(q0, scale(R(0.5), slope_0))), phi0,
+        const vec4<R> f_plus = hll_flux<R, PERT, GAMMA, THERMAL>(P, sanitise(P, add(q0, scale(R(0.5), slope_0))), phi0,
                                         sanitise(P, sub(qp1, scale(R(0.5), slope_p1))), phi_p, axis);
         flux_div = add(flux_div, scale(P.inv_dx, sub(f_plus, f_minus)));
     }
@@ -367,12 +455,20 @@ void step_cell(const SimParams<R> &P, const StageParams<R> &S, const R *field_n,
     const R dphi_proper = gam * (pi0 + (q0.x * grad[0] + q0.y * grad[1] + q0.z * grad[2]));
     const R drag = P.eta * dphi_proper;
     const R d_phi = pi0;
-    const R d_pi = laplacian - dpotential(P, phi0) - drag;
+    // thermal potential: dV/dphi at the cell's temperature eos_temperature(q0.w,
+    // phi0) (docs/EOS.md:133-135), and its plasma part exchanged like the drag
+    R dpot = dpotential(P, phi0), src = drag;
+    if (THERMAL) {
+        const R T0 = thermal_temperature(P, q0.w, phi0);
+        dpot = thermal_dpotential(P, phi0, T0);
+        src = drag + thermal_exchange(phi0, T0);
+    }
+    const R d_pi = laplacian - dpot - drag;
     vec4<R> d_fluid{-flux_div.x, -flux_div.y, -flux_div.z, -flux_div.w};
-    d_fluid.x = d_fluid.x + drag * pi0;
-    d_fluid.y = d_fluid.y - drag * grad[0];
-    d_fluid.z = d_fluid.z - drag * grad[1];
-    d_fluid.w = d_fluid.w - drag * grad[2];
+    d_fluid.x = d_fluid.x + src * pi0;
+    d_fluid.y = d_fluid.y - src * grad[0];
+    d_fluid.z = d_fluid.z - src * grad[1];
+    d_fluid.w = d_fluid.w - src * grad[2];
     const R fu_x = phi0 + S.dt_stage * d_phi;
     const R fu_y = pi0 + S.dt_stage * d_pi;
     const vec4<R> uin = ld4(fluid_in, i0);
@@ -493,7 +589,7 @@ void nucleate_all(const SimParams<R> &P, const float *bubbles, uint32_t count, R
     }
 }
 
-template <typename R, bool PERT = false, bool GAMMA = false>
+template <typename R, bool PERT = false, bool GAMMA = false, bool THERMAL = false>
 void step_all(const SimParams<R> &P, const StageParams<R> &S, const R *field_n, const R *fluid_n,
               const R *field_in, const R *fluid_in, const R *prim, R *field_out, R *fluid_out) {
     const int nx = (int)P.nx, ny = (int)P.ny, nz = (int)P.nz;
@@ -501,15 +597,16 @@ void step_all(const SimParams<R> &P, const StageParams<R> &S, const R *field_n, 
     for (int z = 0; z < nz; ++z)
         for (int y = 0; y < ny; ++y)
             for (int x = 0; x < nx; ++x)
-                step_cell<R, PERT, GAMMA>(P, S, field_n, fluid_n, field_in, fluid_in, prim, field_out, fluid_out, x, y, z);
+                step_cell<R, PERT, GAMMA, THERMAL>(P, S, field_n, fluid_n, field_in, fluid_in, prim, field_out,
+                                                   fluid_out, x, y, z);
 }
 
-template <typename R, bool PERT = false, bool GAMMA = false>
+template <typename R, bool PERT = false, bool GAMMA = false, bool THERMAL = false>
 void primitives_all(const SimParams<R> &P, const R *field, const R *fluid, R *prim) {
     const size_t n = (size_t)P.nx * P.ny * P.nz;
 #pragma omp parallel for schedule(static)
     for (long long i = 0; i < (long long)n; ++i) {
-        const vec4<R> q = eos_prim_from_cons<R, PERT, GAMMA>(P, ld4(fluid, (size_t)i), field[2 * i]);
+        const vec4<R> q = eos_prim_from_cons<R, PERT, GAMMA, THERMAL>(P, ld4(fluid, (size_t)i), field[2 * i]);
         prim[4 * i] = q.x;
         prim[4 * i + 1] = q.y;
         prim[4 * i + 2] = q.z;
@@ -534,7 +631,7 @@ void init_all(const SimParams<R> &P, R *field, R *fluid) {
 // partial per z-plane, planes folded in order.
 // PERT: e_total and e_lab miss e_bg per cell (the caller adds N e_bg in FP64);
 // the kinetic term adds e_bg + p_bg back.
-template <typename R, bool PERT = false>
+template <typename R, bool PERT = false, bool THERMAL = false>
 void reduce_all(const SimParams<R> &P, const R *field, const R *fluid, const R *prim, double sums[4],
                 R *max_v) {
     const int nx = (int)P.nx, ny = (int)P.ny, nz = (int)P.nz;
@@ -561,7 +658,9 @@ void reduce_all(const SimParams<R> &P, const R *field, const R *fluid, const R *
                 const R e_lab = wmax(fluid[4 * i], P.e_floor);
                 const vec4<R> q = ld4(prim, i);
                 const R v2 = q.x * q.x + q.y * q.y + q.z * q.z;
-                const R e_total = R(0.5) * pi * pi + R(0.5) * grad2 + potential(P, phi) + e_lab;
+                // thermal potential: the field holds V(phi, 0), E the rest
+                const R pot = THERMAL ? thermal_potential0(P, phi) : potential(P, phi);
+                const R e_total = R(0.5) * pi * pi + R(0.5) * grad2 + pot + e_lab;
                 const R broken = phi > R(0.5) * P.phi_b ? R(1.0) : R(0.0);
                 const R kinetic = PERT ? ((e_lab + q.w) + (P.e_ref + P.e_ref / R(3.0))) * v2 : (e_lab + q.w) * v2;
                 a0 += (double)e_total;
@@ -626,7 +725,7 @@ inline float f16_to_f32(uint16_t h) {
 
 // vis main (shaders/vis.wgsl:30-55) over a primitives buffer from
 // primitives_all; out = nx*ny*nz half4 texels.
-template <typename R, bool PERT = false>
+template <typename R, bool PERT = false, bool THERMAL = false>
 void vis_all(const SimParams<R> &P, const R *field, const R *fluid, const R *prim, uint16_t *out) {
     const int64_t n = (int64_t)P.nx * P.ny * P.nz;
 #pragma omp parallel for schedule(static)
@@ -646,7 +745,7 @@ void vis_all(const SimParams<R> &P, const R *field, const R *fluid, const R *pri
             a = P.a_rad * (R(1.0) + (R(g_eos_dof) - R(1.0)) * smooth);
         }
         const R x = R(3.0) * pt / a;  // eos_temperature (shaders/eos.wgsl:65-69)
-        const R temp = std::sqrt(std::sqrt(x));
+        const R temp = THERMAL ? thermal_temperature(P, pt, phi) : std::sqrt(std::sqrt(x));
         const R kinetic = (e_lab + p) * vv;
         out[4 * i + 0] = f32_to_f16((float)(phi / P.phi_b));
         out[4 * i + 1] = f32_to_f16((float)speed);
@@ -1020,6 +1119,33 @@ void oracle_step_gamma_f32(const SimParams<float> *P, const StageParams<float> *
                            const float *fluid_n, const float *field_in, const float *fluid_in, const float *prim,
                            float *field_out, float *fluid_out) {
     step_all<float, false, true>(*P, *S, field_n, fluid_n, field_in, fluid_in, prim, field_out, fluid_out);
+}
+
+// Thermal potential constants of the following *_thermal_f32 calls.
+void oracle_set_thermal(float k, float g, float h, float a, float lo, float i2a) {
+    g_th_k = k;
+    g_th_g = g;
+    g_th_h = h;
+    g_th_a = a;
+    g_th_lo = lo;
+    g_th_i2a = i2a;
+}
+void oracle_init_thermal_f32(const SimParams<float> *P, float *field, float *fluid) { init_all(*P, field, fluid); }
+void oracle_primitives_thermal_f32(const SimParams<float> *P, const float *field, const float *fluid, float *prim) {
+    primitives_all<float, false, false, true>(*P, field, fluid, prim);
+}
+void oracle_step_thermal_f32(const SimParams<float> *P, const StageParams<float> *S, const float *field_n,
+                             const float *fluid_n, const float *field_in, const float *fluid_in, const float *prim,
+                             float *field_out, float *fluid_out) {
+    step_all<float, false, false, true>(*P, *S, field_n, fluid_n, field_in, fluid_in, prim, field_out, fluid_out);
+}
+void oracle_reduce_thermal_f32(const SimParams<float> *P, const float *field, const float *fluid,
+                               const float *prim, double *sums, float *max_v) {
+    reduce_all<float, false, true>(*P, field, fluid, prim, sums, max_v);
+}
+void oracle_vis_thermal_f32(const SimParams<float> *P, const float *field, const float *fluid, const float *prim,
+                            uint16_t *out) {
+    vis_all<float, false, true>(*P, field, fluid, prim, out);
 }
 
 double oracle_tanh_f64(double x) { return oracle_tanh(x); }

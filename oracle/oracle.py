@@ -79,6 +79,12 @@ def lib() -> ctypes.CDLL:
         L.oracle_set_eos.argtypes = [ctypes.c_float] * 3
         L.oracle_primitives_gamma_f32.argtypes = [P, P, P, P]
         L.oracle_step_gamma_f32.argtypes = [P] * 9
+        L.oracle_set_thermal.argtypes = [ctypes.c_float] * 6
+        L.oracle_init_thermal_f32.argtypes = [P, P, P]
+        L.oracle_primitives_thermal_f32.argtypes = [P, P, P, P]
+        L.oracle_step_thermal_f32.argtypes = [P] * 9
+        L.oracle_reduce_thermal_f32.argtypes = [P, P, P, P, P, P]
+        L.oracle_vis_thermal_f32.argtypes = [P] * 5
         L.oracle_render.argtypes = [P, P] + [ctypes.c_int] * 6 + [P]
         L.oracle_f32_to_f16.argtypes = [ctypes.c_float]
         L.oracle_f32_to_f16.restype = ctypes.c_uint16
@@ -294,6 +300,14 @@ RK3_F64 = [(0.0, 1.0), (0.75, 0.25), (1.0 / 3.0, 2.0 / 3.0)]
 # ---------------------------------------------------------------------------
 #  Simulation driver over the C kernels
 # ---------------------------------------------------------------------------
+def thermal_constants(a_rad, gamma, a_cubic):
+    """The thermal potential's constants as the library's host rounds them
+    (binary32): a/3, gamma, A/3, A, sqrt(3 gamma / (4a)), 1/(2a)."""
+    a, g, A = f32(a_rad), f32(gamma), f32(a_cubic)
+    return (f32(a / f32(3.0)), g, f32(A / f32(3.0)), A,
+            f32(np.sqrt(f32(f32(f32(3.0) * g) / f32(f32(4.0) * a)))), f32(f32(1.0) / f32(f32(2.0) * a)))
+
+
 def _sim_params(dtype, m: dict, grid, time=0.0) -> np.ndarray:
     d = derived(m)
     fields = [f32(m["dx"]), f32(f32(1.0) / f32(m["dx"])), d["dt"], f32(m["eta"]),
@@ -329,10 +343,12 @@ class OracleSim:
         """precision: "f32", "f64", or "pert" (FP32 perturbation form: the
         fluid energy stored as E - e_ref, include/bubble.h
         BUBBLE_PRECISION_PERTURBATION without its FP64 fallback).
-        eos: ("bag", -, -), ("bag_dof", ratio, -) or ("gamma_law", Gamma, e0)
-        (include/bubble.h BUBBLE_EOS_*; the gamma law in FP32 only)."""
+        eos: ("bag", -, -), ("bag_dof", ratio, -), ("gamma_law", Gamma, e0) or
+        ("thermal", gamma, A) (include/bubble.h BUBBLE_EOS_*; the gamma law and
+        the thermal potential in FP32 only)."""
         self.eos = (eos[0], f32(eos[1]), f32(eos[2]))
         self.gamma = eos[0] == "gamma_law"
+        self.thermal = eos[0] == "thermal"
         self.model = dict(DEFAULT_MODEL, **(model or {}))
         err = validate(self.model)
         if err:
@@ -344,6 +360,8 @@ class OracleSim:
         self.sfx = "f64" if precision == "f64" else "f32"
         self.ksfx = "pert_f32" if self.pert else self.sfx  # kernels that differ in the perturbation form
         self.gsfx = "gamma_f32" if self.gamma else self.ksfx  # kernels that differ for the gamma law
+        if self.thermal:  # every kernel but init and nucleation differs for the thermal potential
+            self.gsfx = self.ksfx = "thermal_f32"
         self.d = derived(self.model)
         self.P = _sim_params(self.dtype, self.model, self.grid)
         self.field = np.zeros((3, self.n, 2), dtype=self.dtype)
@@ -402,6 +420,8 @@ class OracleSim:
         e0 = b if kind == "gamma_law" else f32(0.0)
         dof = a if kind == "bag_dof" else f32(1.0)
         lib().oracle_set_eos(float(c2), float(e0), float(dof))
+        if kind == "thermal":
+            lib().oracle_set_thermal(*[float(x) for x in thermal_constants(self.d["a_rad"], a, b)])
 
     # record_step (src/gpu/sim.rs:881-916)
     def record_step(self):
