@@ -350,10 +350,12 @@ int Batch::ensure_capacity(size_t n, std::string &err) {
 
 // Chooses the z chunks of the batch by timing the batch itself.  The
 // candidates are each size's single-lattice optimum (tuned for filling the
-// GPU with one lattice) and uniform caps (whole columns, 64, 32 planes),
-// which trade the 5-plane prologue of every chunk against load balance once
-// the batch fills the GPU.  The lattices are still in their quiescent
-// initial state, an exact fixed point, so the timing steps change nothing.
+// GPU with one lattice) and caps (whole columns, then 96, 64, 48, 32 and 24
+// planes, each column cut into equal chunks no longer than the cap), which
+// trade the 5-plane prologue of every chunk against the tail of each
+// stage's round once the batch fills the GPU.  The lattices are still in
+// their quiescent initial state, an exact fixed point, so the timing steps
+// change nothing.
 int Batch::autotune(std::string &err) {
     std::vector<std::vector<int>> cands;
     std::vector<int> single;
@@ -363,10 +365,14 @@ int Batch::autotune(std::string &err) {
         single.push_back(lz);
     }
     cands.push_back(single);
-    for (int cap : {1 << 30, 64, 32}) {
+    for (int cap : {1 << 30, 96, 64, 48, 32, 24}) {
         std::vector<int> c;
-        for (auto &L : lats_) c.push_back((int)std::min<uint32_t>(L.grid[2], (uint32_t)cap));
-        cands.push_back(c);
+        for (auto &L : lats_) {
+            const int nz = (int)L.grid[2];
+            const int pieces = (nz + cap - 1) / cap;
+            c.push_back((nz + pieces - 1) / pieces);
+        }
+        if (std::find(cands.begin(), cands.end(), c) == cands.end()) cands.push_back(c);
     }
     cudaEvent_t e0, e1;
     BATCH_CUDA(cudaEventCreate(&e0), "cudaEventCreate");
