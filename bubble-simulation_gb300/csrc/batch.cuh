@@ -100,8 +100,11 @@ __global__ void __launch_bounds__(V2Layout<float, TY>::NT, V2Layout<float, TY>::
                 A.dt = B.dt;
                 A.stage = stage;
                 const LatticeParams<float> P = B.P;
-                if (!v2_item<float, FAST, false, TY>(smem, A, P, B.lz, &B.maps[in_slot], B.tma_ok, status,
-                                                     local % B.tiles_xy, local / B.tiles_xy)) {
+                // prologue loads two planes at a time (one in the strict
+                // arithmetic): the persistent loop's own state leaves no
+                // registers for four
+                if (!v2_item<float, FAST, false, TY, FAST ? 2 : 1>(smem, A, P, B.lz, &B.maps[in_slot], B.tma_ok,
+                                                                   status, local % B.tiles_xy, local / B.tiles_xy)) {
                     // record where the stage's bounded wait gave up (status[8..12])
                     if (threadIdx.x == 0 && atomicCAS(&status[8], 0, 1) == 0) {
                         status[9] = item;

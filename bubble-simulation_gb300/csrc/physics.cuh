@@ -73,6 +73,9 @@ BUBBLE_DEV float2 p_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
 BUBBLE_DEV float2 p_sub(float2 a, float2 b) { return __ffma2_rn(b, bc2(-1.0f), a); }
 BUBBLE_DEV float2 p_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
 BUBBLE_DEV float2 p_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// x^2 + y^2 + z^2 with fixed roundings (the FAST mode's contraction of it)
+BUBBLE_DEV float dot3_rn(float x, float y, float z) { return __fmaf_rn(z, z, __fmaf_rn(y, y, __fmul_rn(x, x))); }
+BUBBLE_DEV double dot3_rn(double x, double y, double z) { return __fma_rn(z, z, __fma_rn(y, y, __dmul_rn(x, x))); }
 
 // ---------------------------------------------------------------------------
 //  Potential (shaders/potential.wgsl:38-47)
@@ -121,19 +124,22 @@ BUBBLE_DEV V4<R> prim_from_cons(const V4<R> &u, const LatticeParams<R> &P) {
     R zx = u.y, zy = u.z, zz = u.w;
     const R zcap = P.z_max * e_lab;
     if constexpr (FAST) {
-        const R z2raw = zx * zx + zy * zy + zz * zz;
-        if (z2raw > zcap * zcap) {
-            const R s = zcap * rsqrt_approx(z2raw);
-            zx *= s;
-            zy *= s;
-            zz *= s;
+        // Explicit roundings (no contraction left to the compiler): the
+        // recovery runs at two sites of the stage kernel (chunk prologue and
+        // z-march), which must give the same bits for every z chunking.
+        R z2 = dot3_rn(zx, zy, zz);
+        if (z2 > __fmul_rn(zcap, zcap)) {
+            const R s = __fmul_rn(zcap, rsqrt_approx(z2));
+            zx = __fmul_rn(zx, s);
+            zy = __fmul_rn(zy, s);
+            zz = __fmul_rn(zz, s);
+            z2 = dot3_rn(zx, zy, zz);
         }
-        const R z2 = zx * zx + zy * zy + zz * zz;
-        const R disc = vmax(R(4.0) * e_lab * e_lab - R(3.0) * z2, R(0.0));
-        R p = (e_lab * e_lab - z2) * rcp_approx(e_lab + sqrt_approx(disc));
+        const R disc = vmax(__fmaf_rn(__fmul_rn(R(4.0), e_lab), e_lab, __fmul_rn(R(-3.0), z2)), R(0.0));
+        R p = __fmul_rn(__fmaf_rn(e_lab, e_lab, -z2), rcp_approx(__fadd_rn(e_lab, sqrt_approx(disc))));
         p = vmax(p, P.p_floor);
-        const R inv = rcp_approx(vmax(e_lab + p, R(1e-30)));
-        return V4<R>{zx * inv, zy * inv, zz * inv, p};
+        const R inv = rcp_approx(vmax(__fadd_rn(e_lab, p), R(1e-30)));
+        return V4<R>{__fmul_rn(zx, inv), __fmul_rn(zy, inv), __fmul_rn(zz, inv), p};
     } else {
         const R zlen = sqrt(zx * zx + zy * zy + zz * zz);
         if (zlen > zcap) {
@@ -153,23 +159,42 @@ BUBBLE_DEV V4<R> prim_from_cons(const V4<R> &u, const LatticeParams<R> &P) {
 
 // FP64 recovery of one FP32 cell, used where the Lorentz factor exceeds 3
 // (v^2 > 8/9), the regime where E^2 - Z^2 cancels.
+template <bool FAST = false>
 BUBBLE_DEV V4<float> prim_from_cons_f64(const V4<float> &u, const LatticeParams<float> &P) {
     const double e_lab = fmax((double)u.x, (double)P.e_floor);
     double zx = u.y, zy = u.z, zz = u.w;
-    const double zcap = (double)P.z_max * e_lab;
-    const double zlen = sqrt(zx * zx + zy * zy + zz * zz);
-    if (zlen > zcap) {
-        const double s = zcap / fmax(zlen, 1e-30);
-        zx *= s;
-        zy *= s;
-        zz *= s;
+    if constexpr (FAST) {
+        // explicit roundings, so every call site computes the same bits
+        const double zcap = __dmul_rn((double)P.z_max, e_lab);
+        const double zlen = __dsqrt_rn(dot3_rn(zx, zy, zz));
+        if (zlen > zcap) {
+            const double s = __ddiv_rn(zcap, fmax(zlen, 1e-30));
+            zx = __dmul_rn(zx, s);
+            zy = __dmul_rn(zy, s);
+            zz = __dmul_rn(zz, s);
+        }
+        const double z2 = dot3_rn(zx, zy, zz);
+        const double disc = fmax(__fma_rn(__dmul_rn(4.0, e_lab), e_lab, __dmul_rn(-3.0, z2)), 0.0);
+        double p = __ddiv_rn(__fma_rn(e_lab, e_lab, -z2), __dadd_rn(e_lab, __dsqrt_rn(disc)));
+        p = fmax(p, (double)P.p_floor);
+        const double s = fmax(__dadd_rn(e_lab, p), 1e-30);
+        return V4<float>{(float)__ddiv_rn(zx, s), (float)__ddiv_rn(zy, s), (float)__ddiv_rn(zz, s), (float)p};
+    } else {
+        const double zcap = (double)P.z_max * e_lab;
+        const double zlen = sqrt(zx * zx + zy * zy + zz * zz);
+        if (zlen > zcap) {
+            const double s = zcap / fmax(zlen, 1e-30);
+            zx *= s;
+            zy *= s;
+            zz *= s;
+        }
+        const double z2 = zx * zx + zy * zy + zz * zz;
+        const double disc = fmax(4.0 * e_lab * e_lab - 3.0 * z2, 0.0);
+        double p = (e_lab * e_lab - z2) / (e_lab + sqrt(disc));
+        p = fmax(p, (double)P.p_floor);
+        const double s = fmax(e_lab + p, 1e-30);
+        return V4<float>{(float)(zx / s), (float)(zy / s), (float)(zz / s), (float)p};
     }
-    const double z2 = zx * zx + zy * zy + zz * zz;
-    const double disc = fmax(4.0 * e_lab * e_lab - 3.0 * z2, 0.0);
-    double p = (e_lab * e_lab - z2) / (e_lab + sqrt(disc));
-    p = fmax(p, (double)P.p_floor);
-    const double s = fmax(e_lab + p, 1e-30);
-    return V4<float>{(float)(zx / s), (float)(zy / s), (float)(zz / s), (float)p};
 }
 
 // ---------------------------------------------------------------------------
@@ -445,7 +470,7 @@ BUBBLE_DEV V4<R> recover(const V4<R> &u, const LatticeParams<R> &P, R phi = R(0)
         V4<R> q = prim_from_cons<R, FAST>(u, P);
         if constexpr (MODE == kMixed) {
             const R v2 = q.x * q.x + q.y * q.y + q.z * q.z;
-            if (v2 > R(8.0) / R(9.0)) q = prim_from_cons_f64(u, P);
+            if (v2 > R(8.0) / R(9.0)) q = prim_from_cons_f64<FAST>(u, P);
         }
         return q;
     }
@@ -466,6 +491,32 @@ BUBBLE_DEV V4<R> sanitise(const V4<R> &q, R p_floor, R vmax2) {
         vz = vz * s;
     }
     return V4<R>{vx, vy, vz, p};
+}
+
+// sanitise(recover(u)) of one staged cell.  The fast bag forms reuse the
+// |v|^2 of the Lorentz-factor test for the clamp (the same values).
+template <typename R, bool FAST, int MODE>
+BUBBLE_DEV V4<R> recover_sanitised(const V4<R> &u, const LatticeParams<R> &P, R phi, R vmax2) {
+    if constexpr (FAST && sizeof(R) == 4 && (MODE == kPlain || MODE == kMixed)) {
+        V4<R> q = prim_from_cons<R, FAST>(u, P);
+        R v2 = dot3_rn(q.x, q.y, q.z);
+        if constexpr (MODE == kMixed) {
+            if (v2 > R(8.0) / R(9.0)) {
+                q = prim_from_cons_f64<true>(u, P);
+                v2 = dot3_rn(q.x, q.y, q.z);
+            }
+        }
+        q.w = vmax(q.w, P.p_floor);
+        if (v2 > vmax2) {
+            const R s = __fsqrt_rn(__fdiv_rn(vmax2, vmax(v2, R(1e-30))));
+            q.x = __fmul_rn(q.x, s);
+            q.y = __fmul_rn(q.y, s);
+            q.z = __fmul_rn(q.z, s);
+        }
+        return q;
+    } else {
+        return sanitise(recover<R, FAST, MODE>(u, P, phi), P.p_floor, vmax2);
+    }
 }
 
 template <typename R>
@@ -490,7 +541,8 @@ BUBBLE_DEV V4<R> half_step(const V4<R> &q, const V4<R> &s, R sign) {
 
 // The two sanitised face states of a cell along one axis from its
 // neighbours qm, qp: lo = q - s/2 (face i-1/2), hi = q + s/2 (face i+1/2),
-// s the MC-limited slope (shaders/step.wgsl:125-144).
+// s the MC-limited slope (shaders/step.wgsl:125-144).  The fast states floor
+// the pressure only; their velocity clamp happens in face_side<FAST>.
 template <typename R, bool FAST>
 BUBBLE_DEV void face_states(const V4<R> &qm, const V4<R> &q, const V4<R> &qp, R p_floor, R vmax2, V4<R> &lo,
                             V4<R> &hi) {
@@ -508,8 +560,11 @@ BUBBLE_DEV void face_states(const V4<R> &qm, const V4<R> &q, const V4<R> &qp, R 
                                       pa.y > 0.0f ? copysignf(fminf(fabsf(ha.y), ma.y), dma.y) : 0.0f);
         const float2 sb = make_float2(pb.x > 0.0f ? copysignf(fminf(fabsf(hb.x), mb.x), dmb.x) : 0.0f,
                                       pb.y > 0.0f ? copysignf(fminf(fabsf(hb.y), mb.y), dmb.y) : 0.0f);
-        lo = sanitise(v4of(p_fma(sa, bc2(-0.5f), qa), p_fma(sb, bc2(-0.5f), qb)), p_floor, vmax2);
-        hi = sanitise(v4of(p_fma(sa, bc2(0.5f), qa), p_fma(sb, bc2(0.5f), qb)), p_floor, vmax2);
+        // pressure floor only: face_side<FAST> applies the velocity clamp
+        lo = v4of(p_fma(sa, bc2(-0.5f), qa), p_fma(sb, bc2(-0.5f), qb));
+        hi = v4of(p_fma(sa, bc2(0.5f), qa), p_fma(sb, bc2(0.5f), qb));
+        lo.w = vmax(lo.w, p_floor);
+        hi.w = vmax(hi.w, p_floor);
     } else {
         const V4<R> s = limit_slope4<R, FAST>(v4_sub(q, qm), v4_sub(qp, q));
         lo = sanitise(half_step(q, s, R(-1)), p_floor, vmax2);
@@ -546,10 +601,25 @@ template <int AXIS, typename R, bool FAST, int FORM = kPlain>
 BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2, const LatticeParams<R> &P, R phi = R(0)) {
     constexpr bool PERT = FORM == kPert;
     FaceSide<R> s;
-    const R vx = q.x, vy = q.y, vz = q.z, p = q.w;
+    R vx = q.x, vy = q.y, vz = q.z;
+    const R p = q.w;
+    R v2raw = vx * vx + vy * vy + vz * vz;
+    if constexpr (FAST) {
+        // The velocity half of sanitise (shaders/step.wgsl:61-72): the fast
+        // face states floor only the pressure and leave the velocity clamp to
+        // this point, where |v|^2 is needed anyway (same values, one |v|^2
+        // per face state instead of two).
+        if (v2raw > zmax2) {
+            const R sc = sqrt(zmax2 / vmax(v2raw, R(1e-30)));
+            vx = vx * sc;
+            vy = vy * sc;
+            vz = vz * sc;
+            v2raw = vx * vx + vy * vy + vz * vz;
+        }
+    }
+    const R v2 = vmin(v2raw, zmax2);
+    const R vd = AXIS == 0 ? vx : (AXIS == 1 ? vy : vz);
     if constexpr (FORM == kGamma || FORM == kThermal) {
-        const R vd = comp<AXIS>(q);
-        const R v2 = vmin(vx * vx + vy * vy + vz * vz, zmax2);
         R cs2, enth;
         if constexpr (FORM == kThermal) {
             const R T = thermal_temperature<R, FAST>(p, phi, P);
@@ -588,8 +658,6 @@ BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2, const LatticeParams<R>
         return s;
     }
     const R pf = PERT ? P.p_bg + p : p;  // the full pressure
-    const R vd = comp<AXIS>(q);
-    const R v2 = vmin(vx * vx + vy * vy + vz * vz, zmax2);
     const R cs2 = R(1.0) / R(3.0);  // eos_sound_speed2 (eos.wgsl:50-53)
     if constexpr (FAST) {
         // 1 - vd^2 - cs2 (v^2 - vd^2) = 1 - (2/3) vd^2 - v^2/3 for cs2 = 1/3;

@@ -171,7 +171,9 @@ BUBBLE_DEV void cross_item(int k, int &i, int &j) {
 // when a bounded wait expired (bit 0 of *status is set); the CTA must then
 // stop.  Usable repeatedly by one CTA: it starts with a barrier and leaves
 // no copy in flight.
-template <typename R, bool FAST, int MIXED, int TY>
+// QBP: planes whose prologue loads are issued together (FP32; FP64 stages
+// one at a time).
+template <typename R, bool FAST, int MIXED, int TY, int QBP = 4>
 BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const LatticeParams<R> &P, int lz,
                         const StageMaps *maps, int tma_ok, int *status, int tile_xy, int chunk) {
     using L = V2Layout<R, TY>;
@@ -215,6 +217,42 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
         fence_mbar_init();
     }
 
+    // ---- static work plan --------------------------------------------------
+    // Thread t takes the items k = t + r NT (r = 0, 1, ...) of each phase, the
+    // same on every plane.  The kinds of item are contiguous ranges of k, so
+    // the slot r meets only the kinds whose range intersects [r NT, (r+1) NT):
+    // with r unrolled those are known at compile time, and each item's indices
+    // are decoded once here instead of on every plane.
+    constexpr int NRX = (L::X_TOTAL + NT - 1) / NT;
+    constexpr int NRY = (L::Y_TOTAL + NT - 1) / NT;
+    constexpr int NRA = (L::A_REAL + NT - 1) / NT;  // slots holding staged cells
+    // own cell of the combine (k = t < NC)
+    const int ci = t % TX, cj = t / TX;
+    const bool c_valid = t < NC && ci < xe && cj < ye;
+    const int cc = (cj + 2) * PW + (ci + 2);
+    const uint32_t c_off = (uint32_t)(y0 + cj) * (uint32_t)P.nx + (uint32_t)(x0 + ci);
+    // Staged cells (the Y-phase primitive items and the per-element copies):
+    // ya_c = the cell in the cross-shaped halo layout, -1 outside the tile's
+    // cells; ya_g = the same cell within a lattice plane, periodic wrap applied.
+    int ya_c[NRY];
+    uint32_t ya_g[NRA];
+    static_for<0, NRY>([&](auto rc) {
+        constexpr int r = decltype(rc)::value;
+        ya_c[r] = -1;
+        if constexpr (r < NRA) {
+            ya_g[r] = 0;
+            const int k = t + r * NT;
+            if (k < L::A_REAL) {
+                int i, j;
+                cross_item<TX, TY, PW>(k, i, j);
+                if (i < xe + 4 && j < ye + 4) {
+                    ya_c[r] = j * PW + i;
+                    ya_g[r] = (uint32_t)wrap1(y0 - 2 + j, P.ny) * (uint32_t)P.nx + (uint32_t)wrap1(x0 - 2 + i, P.nx);
+                }
+            }
+        }
+    });
+
     // Stage raw plane p (p >= z0+3) asynchronously.
     auto issue = [&](int p) {
         const int s = raw_slot(p);
@@ -228,16 +266,14 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
             }
         } else {
             const size_t base = (size_t)gz * plane;
-            for (int k = t; k < L::A_REAL; k += NT) {
-                int i, j;
-                cross_item<TX, TY, PW>(k, i, j);
-                if (i >= xe + 4 || j >= ye + 4) continue;
-                const int gx = wrap1(x0 - 2 + i, P.nx);
-                const int gy = wrap1(y0 - 2 + j, P.ny);
-                const size_t g = base + (size_t)gy * P.nx + gx;
-                cp_async_v4(raw_u + s * PC + j * PW + i, A.fluid_in + g);
-                cp_async_v2(raw_f + s * PC + j * PW + i, A.field_in + g);
-            }
+            static_for<0, NRA>([&](auto rc) {
+                constexpr int r = decltype(rc)::value;
+                const int c = ya_c[r];
+                if (c >= 0) {
+                    cp_async_v4(raw_u + s * PC + c, A.fluid_in + base + ya_g[r]);
+                    cp_async_v2(raw_f + s * PC + c, A.field_in + base + ya_g[r]);
+                }
+            });
             cp_async_commit();
         }
     };
@@ -251,23 +287,42 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
         return true;
     };
 
-    // Synchronous staging used by the prologue (planes z0-2 .. z0+2).
-    auto stage_plane_sync = [&](int p) {
-        const int gz = wrap1(p, P.nz);
-        const size_t base = (size_t)gz * plane;
-        V4<R> *pr = prim_slot(p);
-        R *ph = phi_slot(p);
-        for (int k = t; k < L::A_REAL; k += NT) {
-            int i, j;
-            cross_item<TX, TY, PW>(k, i, j);
-            if (i >= xe + 4 || j >= ye + 4) continue;
-            const int gx = wrap1(x0 - 2 + i, P.nx);
-            const int gy = wrap1(y0 - 2 + j, P.ny);
-            const size_t g = base + (size_t)gy * P.nx + gx;
-            const V4<R> u = A.fluid_in[g];
-            const R phv = A.field_in[g].x;
-            ph[j * PW + i] = phv;
-            pr[j * PW + i] = sanitise(recover<R, FAST, MIXED>(u, P, phv), P.p_floor, zmax2);
+    // Synchronous staging of the prologue: the loads of NQ <= QB planes
+    // p .. p+NQ-1 are all issued before the first is used.
+    constexpr int QB = sizeof(R) == 4 ? QBP : 1;
+    static_assert(4 % QB == 0, "the prologue stages four planes");
+    struct Staged {
+        V4<R> u[QB][NRA];
+        R phi[QB][NRA];
+    };
+    auto load_planes = [&](int p, Staged &S, auto nq) {
+        constexpr int NQ = decltype(nq)::value;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            const size_t base = (size_t)wrap1(p + q, P.nz) * plane;
+            static_for<0, NRA>([&](auto rc) {
+                constexpr int r = decltype(rc)::value;
+                if (ya_c[r] >= 0) {
+                    S.u[q][r] = A.fluid_in[base + ya_g[r]];
+                    S.phi[q][r] = A.field_in[base + ya_g[r]].x;
+                }
+            });
+        }
+    };
+    auto store_planes = [&](int p, const Staged &S, auto nq) {
+        constexpr int NQ = decltype(nq)::value;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            V4<R> *pr = prim_slot(p + q);
+            R *ph = phi_slot(p + q);
+            static_for<0, NRA>([&](auto rc) {
+                constexpr int r = decltype(rc)::value;
+                const int c = ya_c[r];
+                if (c >= 0) {
+                    ph[c] = S.phi[q][r];
+                    pr[c] = recover_sanitised<R, FAST, MIXED>(S.u[q][r], P, S.phi[q][r], zmax2);
+                }
+            });
         }
     };
     auto z_states = [&](int p, int n, V4<R> &lo, V4<R> &hi) {
@@ -278,8 +333,17 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
 
     // ---- prologue ----------------------------------------------------------
     // Planes z0-2 .. z0+1 fill the 4-slot primitive ring; the z face
-    // z0 - 1/2 needs all four.  Plane z0+2 then takes the slot of z0-2.
-    for (int p = z0 - 2; p <= z0 + 1; ++p) stage_plane_sync(p);
+    // z0 - 1/2 needs all four.  Plane z0+2 then takes the slot of z0-2: its
+    // loads are in flight while that face is computed.
+    {
+        Staged S;
+        for (int p = z0 - 2; p <= z0 + 1; p += QB) {
+            load_planes(p, S, std::integral_constant<int, QB>{});
+            store_planes(p, S, std::integral_constant<int, QB>{});
+        }
+    }
+    Staged S2;
+    load_planes(z0 + 2, S2, std::integral_constant<int, 1>{});
     __syncthreads();  // also publishes the mbarrier initialisation
     for (int n = t; n < NC; n += NT) {
         V4<R> lo_m, hi_m, lo_0, hi_0;
@@ -295,42 +359,13 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
         fzs[((z0 - 1 + 8) & 1) * NC + n] = hll_flux<2, R, FAST, MIXED>(hi_m, lo_0, zmax2, P, phl, phr);
     }
     __syncthreads();
-    stage_plane_sync(z0 + 2);
+    store_planes(z0 + 2, S2, std::integral_constant<int, 1>{});
     if (z0 + 3 <= zlast) issue(z0 + 3);
     __syncthreads();
 
     // own-cell state of the plane awaiting its combine, loaded a phase ahead
     V2<R> pf{R(0), R(0)}, pfn{R(0), R(0)};
     V4<R> pu{R(0), R(0), R(0), R(0)}, pun{R(0), R(0), R(0), R(0)};
-
-    // ---- static work plan --------------------------------------------------
-    // Thread t takes the items k = t + r NT (r = 0, 1, ...) of each phase, the
-    // same on every plane.  The kinds of item are contiguous ranges of k, so
-    // the slot r meets only the kinds whose range intersects [r NT, (r+1) NT):
-    // with r unrolled those are known at compile time, and each item's indices
-    // are decoded once here instead of on every plane.
-    constexpr int NRX = (L::X_TOTAL + NT - 1) / NT;
-    constexpr int NRY = (L::Y_TOTAL + NT - 1) / NT;
-    // own cell of the combine (k = t < NC)
-    const int ci = t % TX, cj = t / TX;
-    const bool c_valid = t < NC && ci < xe && cj < ye;
-    const int cc = (cj + 2) * PW + (ci + 2);
-    const uint32_t c_off = (uint32_t)(y0 + cj) * (uint32_t)P.nx + (uint32_t)(x0 + ci);
-    // Y-phase primitive items: shared-memory cell of the cross-shaped halo
-    // layout, -1 outside the tile's cells
-    int ya_c[NRY];
-    static_for<0, NRY>([&](auto rc) {
-        constexpr int r = decltype(rc)::value;
-        ya_c[r] = -1;
-        if constexpr (r * NT < L::A_REAL) {
-            const int k = t + r * NT;
-            if (k < L::A_REAL) {
-                int i, j;
-                cross_item<TX, TY, PW>(k, i, j);
-                if (i < xe + 4 && j < ye + 4) ya_c[r] = j * PW + i;
-            }
-        }
-    });
 
     for (int z = z0;; ++z) {
         // ring slots of this plane, computed once for every item
@@ -374,11 +409,15 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
                     const V4<R> fym = fys[t], fyp = fys[t + TX];
                     const V4<R> fzm = fz_rd_m[t], fzp = fz_rd_p[t];
                     V4<R> fd;
-                    if constexpr (FAST) {
-                        fd.x = ((fxp.x - fxm.x) + (fyp.x - fym.x) + (fzp.x - fzm.x)) * P.inv_dx;
-                        fd.y = ((fxp.y - fxm.y) + (fyp.y - fym.y) + (fzp.y - fzm.y)) * P.inv_dx;
-                        fd.z = ((fxp.z - fxm.z) + (fyp.z - fym.z) + (fzp.z - fzm.z)) * P.inv_dx;
-                        fd.w = ((fxp.w - fxm.w) + (fyp.w - fym.w) + (fzp.w - fzm.w)) * P.inv_dx;
+                    if constexpr (FAST && sizeof(R) == 4) {
+                        // ((dx + dy) + dz) / dx on the (x, y) and (z, w) halves
+                        const float2 fa = p_mul(p_add(p_add(p_sub(lo2(fxp), lo2(fxm)), p_sub(lo2(fyp), lo2(fym))),
+                                                      p_sub(lo2(fzp), lo2(fzm))),
+                                                bc2(P.inv_dx));
+                        const float2 fb = p_mul(p_add(p_add(p_sub(hi2(fxp), hi2(fxm)), p_sub(hi2(fyp), hi2(fym))),
+                                                      p_sub(hi2(fzp), hi2(fzm))),
+                                                bc2(P.inv_dx));
+                        fd = v4of(fa, fb);
                     } else {
                         fd = V4<R>{R(0), R(0), R(0), R(0)};
                         fd.x = fd.x + (fxp.x - fxm.x) * P.inv_dx;
@@ -415,9 +454,31 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
                     const R dZx = -fd.y - src * gx;
                     const R dZy = -fd.z - src * gy;
                     const R dZz = -fd.w - src * gz;
+                    const size_t g = (size_t)zc * plane + c_off;
+                    if constexpr (FAST && sizeof(R) == 4) {
+                        // U_in + dt L and the stage combine, paired
+                        const float2 dt2 = bc2(A.dt), a1 = bc2(A.a1);
+                        const float2 fu = p_fma(dt2, make_float2(pi0, d_pi), make_float2(pf.x, pf.y));
+                        const float2 ua = p_fma(dt2, make_float2(dE, dZx), lo2(pu));
+                        const float2 ub = p_fma(dt2, make_float2(dZy, dZz), hi2(pu));
+                        float2 of, oa, ob;
+                        if (A.stage == 0) {
+                            of = p_mul(a1, fu);
+                            oa = p_mul(a1, ua);
+                            ob = p_mul(a1, ub);
+                        } else {
+                            // rk_combine<FAST>: U^n + a1 (U1 - U^n)
+                            const float2 fn = make_float2(pfn.x, pfn.y);
+                            of = p_fma(a1, p_sub(fu, fn), fn);
+                            oa = p_fma(a1, p_sub(ua, lo2(pun)), lo2(pun));
+                            ob = p_fma(a1, p_sub(ub, hi2(pun)), hi2(pun));
+                        }
+                        A.field_out[g] = V2<R>{of.x, of.y};
+                        A.fluid_out[g] = v4of(oa, ob);
+                        return;
+                    }
                     const V2<R> fu{pf.x + A.dt * pi0, pf.y + A.dt * d_pi};
                     const V4<R> uu{pu.x + A.dt * dE, pu.y + A.dt * dZx, pu.z + A.dt * dZy, pu.w + A.dt * dZz};
-                    const size_t g = (size_t)zc * plane + c_off;
                     if (A.stage == 0) {
                         A.field_out[g] = V2<R>{A.a1 * fu.x, A.a1 * fu.y};
                         A.fluid_out[g] = V4<R>{A.a1 * uu.x, A.a1 * uu.y, A.a1 * uu.z, A.a1 * uu.w};
@@ -508,7 +569,7 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
                     const V4<R> u = raw_ua[c];
                     const R phv = raw_fa[c].x;
                     ph_a[c] = phv;
-                    pr_a[c] = sanitise(recover<R, FAST, MIXED>(u, P, phv), P.p_floor, zmax2);
+                    pr_a[c] = recover_sanitised<R, FAST, MIXED>(u, P, phv, zmax2);
                     return;
                 }
             }
