@@ -92,6 +92,22 @@ def ncu_traffic(wl: str) -> float | None:
     return None
 
 
+def ncu_flops() -> float | None:
+    """FP32 operations per cell-update of the stage kernel from the committed
+    ncu summary (FADD + FMUL + 2 FFMA, paired forms counted per lane), if any."""
+    p = ROOT / "profiles" / "stage_v2_flops.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("fp32_flop_per_cell_update:"):
+            return float(line.split(":")[1])
+    return None
+
+
+# Nominal FP32 (CUDA-core) rate of a GB300: 152 SMs x 128 lanes x 2 (FMA) x 2.07 GHz.
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -604,6 +620,12 @@ def main() -> int:
                 "traffic": (traffic_per_cell * cells / 3) if traffic_per_cell else None,
                 "algorithmic_bytes_per_launch": BYTES_PER_CELL_UPDATE * cells / 3,
                 "kernel": "stage_v2_kernel (3 launches per step)"}
+    flop_per_cell = ncu_flops()
+    fp32 = None
+    if flop_per_cell:
+        tf = flop_per_cell * cells / (ms_per_step * 1e-3) / 1e12
+        fp32 = {"achieved": tf, "unit": "TFLOP/s", "flop_per_cell_update": flop_per_cell,
+                "nominal_peak": FP32_NOMINAL_TFLOPS, "frac_of_nominal": tf / FP32_NOMINAL_TFLOPS}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -617,7 +639,7 @@ def main() -> int:
                 "config": {"workload": wl["name"], "grid": list(wl["grid"]), "cells": cells,
                            "tile": [32, ty, lz], "l2": "inputs larger than L2 (no flush)",
                            "parallelism": f"replicas x{world}" if world > 1 else "single lattice"},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "roofline": roofline, "fp32": fp32, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": launches, "clocks": clocks.summary()}
         print(json.dumps(line), flush=True)
     sim.close()

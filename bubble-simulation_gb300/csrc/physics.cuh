@@ -215,19 +215,20 @@ BUBBLE_DEV V4<R> prim_from_cons_pert(const V4<R> &u, const LatticeParams<R> &P) 
     R zx = u.y, zy = u.z, zz = u.w;
     const R zcap = P.z_max * e_lab;
     if constexpr (FAST) {
-        const R z2raw = zx * zx + zy * zy + zz * zz;
-        if (z2raw > zcap * zcap) {
-            const R sc = zcap * rsqrt_approx(z2raw);
-            zx *= sc;
-            zy *= sc;
-            zz *= sc;
+        // explicit roundings, as prim_from_cons<FAST>: same bits at every call site
+        R z2 = dot3_rn(zx, zy, zz);
+        if (z2 > __fmul_rn(zcap, zcap)) {
+            const R sc = __fmul_rn(zcap, rsqrt_approx(z2));
+            zx = __fmul_rn(zx, sc);
+            zy = __fmul_rn(zy, sc);
+            zz = __fmul_rn(zz, sc);
+            z2 = dot3_rn(zx, zy, zz);
         }
-        const R z2 = zx * zx + zy * zy + zz * zz;
-        const R sq = sqrt_approx(vmax(R(4.0) * e_lab * e_lab - R(3.0) * z2, R(0.0)));
-        R dp = de * R(1.0 / 3.0) - z2 * rcp_approx(sq + R(2.0) * e_lab);
+        const R sq = sqrt_approx(vmax(__fmaf_rn(__fmul_rn(R(4.0), e_lab), e_lab, __fmul_rn(R(-3.0), z2)), R(0.0)));
+        R dp = __fmaf_rn(de, R(1.0 / 3.0), -__fmul_rn(z2, rcp_approx(__fmaf_rn(R(2.0), e_lab, sq))));
         dp = vmax(dp, P.p_floor);
-        const R inv = rcp_approx(vmax(e_lab + P.p_bg + dp, R(1e-30)));
-        return V4<R>{zx * inv, zy * inv, zz * inv, dp};
+        const R inv = rcp_approx(vmax(__fadd_rn(__fadd_rn(e_lab, P.p_bg), dp), R(1e-30)));
+        return V4<R>{__fmul_rn(zx, inv), __fmul_rn(zy, inv), __fmul_rn(zz, inv), dp};
     } else {
         const R zlen = sqrt(zx * zx + zy * zy + zz * zz);
         if (zlen > zcap) {
@@ -246,24 +247,43 @@ BUBBLE_DEV V4<R> prim_from_cons_pert(const V4<R> &u, const LatticeParams<R> &P) 
 }
 
 // FP64 recovery of one FP32 cell in the perturbation form (gamma > 3).
+template <bool FAST = false>
 BUBBLE_DEV V4<float> prim_from_cons_pert_f64(const V4<float> &u, const LatticeParams<float> &P) {
     const double de = fmax((double)u.x, (double)P.e_floor);
     const double e_lab = (double)P.e_bg + de;
     double zx = u.y, zy = u.z, zz = u.w;
-    const double zcap = (double)P.z_max * e_lab;
-    const double zlen = sqrt(zx * zx + zy * zy + zz * zz);
-    if (zlen > zcap) {
-        const double sc = zcap / fmax(zlen, 1e-30);
-        zx *= sc;
-        zy *= sc;
-        zz *= sc;
+    if constexpr (FAST) {
+        // explicit roundings, so every call site computes the same bits
+        const double zcap = __dmul_rn((double)P.z_max, e_lab);
+        const double zlen = __dsqrt_rn(dot3_rn(zx, zy, zz));
+        if (zlen > zcap) {
+            const double sc = __ddiv_rn(zcap, fmax(zlen, 1e-30));
+            zx = __dmul_rn(zx, sc);
+            zy = __dmul_rn(zy, sc);
+            zz = __dmul_rn(zz, sc);
+        }
+        const double z2 = dot3_rn(zx, zy, zz);
+        const double sq = __dsqrt_rn(fmax(__fma_rn(__dmul_rn(4.0, e_lab), e_lab, __dmul_rn(-3.0, z2)), 0.0));
+        double dp = __dsub_rn(__ddiv_rn(de, 3.0), __ddiv_rn(z2, __fma_rn(2.0, e_lab, sq)));
+        dp = fmax(dp, (double)P.p_floor);
+        const double d = fmax(__dadd_rn(__dadd_rn(e_lab, (double)P.p_bg), dp), 1e-30);
+        return V4<float>{(float)__ddiv_rn(zx, d), (float)__ddiv_rn(zy, d), (float)__ddiv_rn(zz, d), (float)dp};
+    } else {
+        const double zcap = (double)P.z_max * e_lab;
+        const double zlen = sqrt(zx * zx + zy * zy + zz * zz);
+        if (zlen > zcap) {
+            const double sc = zcap / fmax(zlen, 1e-30);
+            zx *= sc;
+            zy *= sc;
+            zz *= sc;
+        }
+        const double z2 = zx * zx + zy * zy + zz * zz;
+        const double sq = sqrt(fmax(4.0 * e_lab * e_lab - 3.0 * z2, 0.0));
+        double dp = de / 3.0 - z2 / (sq + 2.0 * e_lab);
+        dp = fmax(dp, (double)P.p_floor);
+        const double d = fmax(e_lab + (double)P.p_bg + dp, 1e-30);
+        return V4<float>{(float)(zx / d), (float)(zy / d), (float)(zz / d), (float)dp};
     }
-    const double z2 = zx * zx + zy * zy + zz * zz;
-    const double sq = sqrt(fmax(4.0 * e_lab * e_lab - 3.0 * z2, 0.0));
-    double dp = de / 3.0 - z2 / (sq + 2.0 * e_lab);
-    dp = fmax(dp, (double)P.p_floor);
-    const double d = fmax(e_lab + (double)P.p_bg + dp, 1e-30);
-    return V4<float>{(float)(zx / d), (float)(zy / d), (float)(zz / d), (float)dp};
 }
 
 // ---------------------------------------------------------------------------
@@ -463,7 +483,7 @@ BUBBLE_DEV V4<R> recover(const V4<R> &u, const LatticeParams<R> &P, R phi = R(0)
         V4<R> q = prim_from_cons_pert<R, FAST>(u, P);
         if constexpr (sizeof(R) == 4) {
             const R v2 = q.x * q.x + q.y * q.y + q.z * q.z;
-            if (v2 > R(8.0) / R(9.0)) q = prim_from_cons_pert_f64(u, P);
+            if (v2 > R(8.0) / R(9.0)) q = prim_from_cons_pert_f64<FAST>(u, P);
         }
         return q;
     } else {
@@ -493,16 +513,18 @@ BUBBLE_DEV V4<R> sanitise(const V4<R> &q, R p_floor, R vmax2) {
     return V4<R>{vx, vy, vz, p};
 }
 
-// sanitise(recover(u)) of one staged cell.  The fast bag forms reuse the
-// |v|^2 of the Lorentz-factor test for the clamp (the same values).
+// sanitise(recover(u)) of one staged cell.  The fast bag and perturbation
+// forms reuse the |v|^2 of the Lorentz-factor test for the clamp (the same
+// values) and round explicitly, so the chunk prologue and the z-march give
+// the same bits.
 template <typename R, bool FAST, int MODE>
 BUBBLE_DEV V4<R> recover_sanitised(const V4<R> &u, const LatticeParams<R> &P, R phi, R vmax2) {
-    if constexpr (FAST && sizeof(R) == 4 && (MODE == kPlain || MODE == kMixed)) {
-        V4<R> q = prim_from_cons<R, FAST>(u, P);
+    if constexpr (FAST && sizeof(R) == 4 && (MODE == kPlain || MODE == kMixed || MODE == kPert)) {
+        V4<R> q = MODE == kPert ? prim_from_cons_pert<R, FAST>(u, P) : prim_from_cons<R, FAST>(u, P);
         R v2 = dot3_rn(q.x, q.y, q.z);
-        if constexpr (MODE == kMixed) {
+        if constexpr (MODE == kMixed || MODE == kPert) {
             if (v2 > R(8.0) / R(9.0)) {
-                q = prim_from_cons_f64<true>(u, P);
+                q = MODE == kPert ? prim_from_cons_pert_f64<true>(u, P) : prim_from_cons_f64<true>(u, P);
                 v2 = dot3_rn(q.x, q.y, q.z);
             }
         }
