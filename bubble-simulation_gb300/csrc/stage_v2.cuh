@@ -110,6 +110,7 @@ BUBBLE_DEV void cp_async_v2(V2<R> *dst, const V2<R> *src) {
 }
 
 constexpr int pad32(int n) { return (n + 31) / 32 * 32; }
+constexpr int round_up(int n, int m) { return (n + m - 1) / m * m; }
 constexpr size_t align128(size_t b) { return (b + 127) / 128 * 128; }
 
 template <typename R, int TY>
@@ -124,6 +125,15 @@ struct V2Layout {
     // phase X: combine of the previous plane, then face states
     static constexpr int X_C = NC, X_Z = NC, X_Y = TX * (TY + 2), X_X = (TX + 2) * TY;
     static constexpr int X_TOTAL = X_C + X_Z + X_Y + X_X;
+    // Where it costs no extra slot, each kind of phase-X item starts at a
+    // multiple of NT, so every unrolled slot holds one kind and the phase's
+    // code holds each item body once.
+    static constexpr bool X_ALIGN = round_up(X_C, NT) + round_up(X_Z, NT) + round_up(X_Y, NT) + X_X <=
+                                    round_up(X_TOTAL, NT);
+    static constexpr int XO_Z = X_ALIGN ? round_up(X_C, NT) : X_C;
+    static constexpr int XO_Y = XO_Z + (X_ALIGN ? round_up(X_Z, NT) : X_Z);
+    static constexpr int XO_X = XO_Y + (X_ALIGN ? round_up(X_Y, NT) : X_Y);
+    static constexpr int X_END = XO_X + X_X;
     // phase Y: primitives of the staged plane, then face fluxes
     static constexpr int A_REAL = TY * PW + 4 * TX;
     static constexpr int Y_A = pad32(A_REAL), Y_Z = NC, Y_Y = TX * (TY + 1), Y_X = (TX + 1) * TY;
@@ -147,7 +157,9 @@ struct V2Layout {
     static constexpr size_t bytes = o_bar + 2 * sizeof(uint64_t);
     static constexpr uint32_t plane_tx_bytes = PC * (sizeof(V4<R>) + sizeof(V2<R>));
     static_assert(NT >= NC, "the combine phase maps one thread per column");
-    static_assert(X_C % 32 == 0 && (X_C + X_Z) % 32 == 0 && (X_C + X_Z + X_Y) % 32 == 0, "warp-uniform X");
+    static_assert(X_C % 32 == 0 && XO_Z % 32 == 0 && (XO_Z + X_Z) % 32 == 0 && XO_Y % 32 == 0 &&
+                      (XO_Y + X_Y) % 32 == 0 && XO_X % 32 == 0,
+                  "warp-uniform X");
     static_assert(Y_A % 32 == 0 && (Y_A + Y_Z) % 32 == 0 && (Y_A + Y_Z + Y_Y) % 32 == 0, "warp-uniform Y");
 };
 
@@ -223,7 +235,7 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
     // the slot r meets only the kinds whose range intersects [r NT, (r+1) NT):
     // with r unrolled those are known at compile time, and each item's indices
     // are decoded once here instead of on every plane.
-    constexpr int NRX = (L::X_TOTAL + NT - 1) / NT;
+    constexpr int NRX = (L::X_END + NT - 1) / NT;
     constexpr int NRY = (L::Y_TOTAL + NT - 1) / NT;
     constexpr int NRA = (L::A_REAL + NT - 1) / NT;  // slots holding staged cells
     // own cell of the combine (k = t < NC)
@@ -494,10 +506,10 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
                 }
             }
             if (z >= z1) return;
-            if constexpr (lo < L::X_C + L::X_Z && hi > L::X_C) {
-                if (k < L::X_C + L::X_Z) {
+            if constexpr (lo < L::XO_Z + L::X_Z && hi > L::XO_Z) {
+                if ((lo >= L::XO_Z || k >= L::XO_Z) && k < L::XO_Z + L::X_Z) {
                     // z face states of plane z+1 (cell n)
-                    const int n = k - L::X_C;
+                    const int n = k - L::XO_Z;
                     const int c = (n / TX + 2) * PW + (n % TX + 2);
                     V4<R> lo_s, hi_s;
                     face_states<R, FAST>(pr_z[c], pr_zp1[c], pr_zp2[c], P.p_floor, zmax2, lo_s, hi_s);
@@ -506,10 +518,10 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
                     return;
                 }
             }
-            if constexpr (lo < L::X_C + L::X_Z + L::X_Y && hi > L::X_C + L::X_Z) {
-                if (k < L::X_C + L::X_Z + L::X_Y) {
+            if constexpr (lo < L::XO_Y + L::X_Y && hi > L::XO_Y) {
+                if ((lo >= L::XO_Y || k >= L::XO_Y) && k < L::XO_Y + L::X_Y) {
                     // y face states of plane z, cell row jj-1
-                    const int q = k - L::X_C - L::X_Z;
+                    const int q = k - L::XO_Y;
                     const int jj = q / TX;
                     const int c = (jj + 1) * PW + (q - jj * TX + 2);
                     V4<R> lo_s, hi_s;
@@ -519,10 +531,10 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
                     return;
                 }
             }
-            if constexpr (hi > L::X_C + L::X_Z + L::X_Y) {
-                if (k < L::X_TOTAL) {
+            if constexpr (hi > L::XO_X) {
+                if ((lo >= L::XO_X || k >= L::XO_X) && k < L::X_END) {
                     // x face states of plane z, cell column ii-1
-                    const int q = k - L::X_C - L::X_Z - L::X_Y;
+                    const int q = k - L::XO_X;
                     const int j = q / (TX + 2);
                     const int c = (j + 2) * PW + (q - j * (TX + 2) + 1);
                     V4<R> lo_s, hi_s;
