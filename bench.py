@@ -393,7 +393,7 @@ def run_serve(args) -> int:
     n = len(reqs)
 
     def serve(policy):
-        srv = bubble.Server(math="fast", chunk_steps=50, policy=policy)
+        srv = bubble.Server(math="fast", chunk_steps=50, policy=policy, chunk_planes=args.chunk_planes)
         base = srv.now()
         arrival_of, i, done = {}, 0, []
         while len(done) < n:
@@ -436,7 +436,7 @@ def run_serve(args) -> int:
             "config": {"workload": f"{n} requests, Poisson 20/s, edges from {{48,64,128,192,256}}, 1-32 bubbles, "
                                    "eta log-U[0.02,1], seed factor U[0.9,1.5], 500-3000 steps, FP32 fast"},
             "p50_latency_s": percentile(lat, 0.5), "p99_latency_s": percentile(lat, 0.99),
-            "cell_updates_per_s": cells / span, "policy": "fifo with backfill, 24 M resident cells",
+            "cell_updates_per_s": cells / span, "policy": "fifo with backfill, 24 M resident cells", "chunk_planes": args.chunk_planes or 64,
             "shortest_first": {"solves_per_s": n / span_sj, "p50_latency_s": percentile(lat_sj, 0.5),
                                "p99_latency_s": percentile(lat_sj, 0.99)},
             "plain": {"solves_per_s": n / (finish - reqs[0][0]), "p50_latency_s": percentile(plain_lat, 0.5),
@@ -524,6 +524,8 @@ def main() -> int:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--lattices", type=int, default=64, help="batch64 workload: number of lattices")
     ap.add_argument("--batch-steps", type=int, default=1000, help="batch64 workload: steps per solve")
+    ap.add_argument("--chunk-planes", type=int, default=0,
+                    help="serve workload: z planes per work item of a lattice (0: the server's default)")
     ap.add_argument("--requests", type=int, default=24, help="serve workload: number of requests")
     ap.add_argument("--study-grid", type=int, default=256, help="precision_study workload: lattice edge")
     ap.add_argument("--study-steps", type=int, default=3000, help="precision_study workload: steps")

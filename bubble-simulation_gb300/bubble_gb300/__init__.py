@@ -467,10 +467,10 @@ class Server:
 
     def __init__(self, math: str = "fast", chunk_steps: int = 50, max_active: int = 64,
                  memory_fraction: float = 0.85, use_graph: bool = True, tile_y: int = 8,
-                 resident_cells: int = 0, policy: str = "fifo"):
+                 resident_cells: int = 0, policy: str = "fifo", chunk_planes: int = 0):
         self._L = load()
         opt = _lib.ServerOptions(_lib.MATH[math], tile_y, chunk_steps, max_active, memory_fraction, int(use_graph),
-                                 resident_cells, _lib.SERVE_POLICY[policy])
+                                 resident_cells, _lib.SERVE_POLICY[policy], chunk_planes)
         h = ctypes.c_void_p()
         check(self._L.bubble_server_create(ctypes.byref(opt), ctypes.byref(h)))
         self._h = h

@@ -86,7 +86,7 @@ class BatchInfo(ctypes.Structure):
 class ServerOptions(ctypes.Structure):
     _fields_ = [("math", ctypes.c_int32), ("tile_y", ctypes.c_int32), ("chunk_steps", ctypes.c_uint32),
                 ("max_active", ctypes.c_uint32), ("memory_fraction", ctypes.c_float), ("use_graph", ctypes.c_int32),
-                ("resident_cells", ctypes.c_uint64), ("policy", ctypes.c_int32)]
+                ("resident_cells", ctypes.c_uint64), ("policy", ctypes.c_int32), ("chunk_planes", ctypes.c_uint32)]
 
 
 SERVE_POLICY = {"fifo": 0, "shortest": 1}

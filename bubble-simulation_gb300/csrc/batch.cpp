@@ -284,7 +284,12 @@ int Batch::add(const bubble_spec &spec, uint32_t *index, std::string &err) {
     L.dt = d.dt;
     L.schedule = make_schedule(spec.nucleation, spec.bubbles, d.seed_radius, L.grid, spec.nucleation_duration,
                                spec.seed);
-    L.lz = (int)std::min<uint32_t>(L.grid[2], (uint32_t)lz_cap_);
+    {
+        // equal chunks no longer than the cap
+        const int nz = (int)L.grid[2];
+        const int pieces = (nz + lz_cap_ - 1) / lz_cap_;
+        L.lz = (nz + pieces - 1) / pieces;
+    }
     const int rc = allocate(L, err);
     if (rc != BUBBLE_OK) return rc;
     lats_.push_back(std::move(L));

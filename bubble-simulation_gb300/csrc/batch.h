@@ -88,6 +88,12 @@ class Batch {
     int ensure_capacity(size_t n, std::string &err);
     int check_status(std::string &err);
 
+   public:
+    // z planes per work item of lattices that join later (0: 64)
+    void set_chunk_planes(int planes) { lz_cap_ = planes > 0 ? planes : 64; }
+
+   private:
+
     std::vector<Lat> lats_;
     std::vector<uint32_t> item_order_;  // active lattices by decreasing size
     int math_ = BUBBLE_MATH_FAST;

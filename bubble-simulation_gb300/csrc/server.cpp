@@ -33,6 +33,7 @@ class Server {
         bo.max_grid = 0;
         const int rc = Batch::create_empty(o.math, &bo, s->batch_, err);
         if (rc != BUBBLE_OK) return rc;
+        s->batch_->set_chunk_planes((int)o.chunk_planes);
         s->t0_ = std::chrono::steady_clock::now();
         out = std::move(s);
         return BUBBLE_OK;
@@ -283,6 +284,7 @@ void bubble_server_options_default(bubble_server_options *out) {
     out->use_graph = 1;
     out->resident_cells = 0;
     out->policy = BUBBLE_SERVE_FIFO;
+    out->chunk_planes = 0;
 }
 
 int bubble_server_create(const bubble_server_options *opt, bubble_server **out) {

@@ -53,14 +53,15 @@ int default_chunk(const uint32_t grid[3], int ty) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long tiles = (long)((grid[0] + 31) / 32) * (long)((grid[1] + ty - 1) / ty);
     // Aim at >= 24 CTAs per SM over the launch (about a dozen waves of two
-    // resident CTAs, so the tail wave is short) while keeping chunks >= 16
-    // planes so the 5-plane prologue stays below a third of the work.
-    // Measured at 512^3: lz = 128 beats 256 by 3 % and 64 by 1 %.
+    // resident CTAs, so the tail wave is short) while keeping chunks >= 32
+    // planes so each chunk's prologue stays a small share of its work.
+    // Measured (ms per step): 512^3 lz 128 13.07, 103 13.11, 64 13.20, 256
+    // 13.45; 256^3 lz 32 1.79, 16 1.84; 128^3 lz 32 0.281, 16 0.293, 64 0.388.
     const long want = (long)sms * 24;
     long chunks = (want + tiles - 1) / tiles;
     if (chunks < 1) chunks = 1;
     long lz = ((long)grid[2] + chunks - 1) / chunks;
-    if (lz < 16) lz = 16;
+    if (lz < 32) lz = 32;
     if (lz > (long)grid[2]) lz = grid[2];
     return (int)lz;
 }

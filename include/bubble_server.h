@@ -42,6 +42,9 @@ typedef struct bubble_server_options {
                                 request that does not fit lets smaller later ones
                                 backfill; BUBBLE_SERVE_SHORTEST: least work
                                 (cells x steps) first                            */
+    uint32_t chunk_planes;   /* z planes per work item of a lattice (0: 64);
+                                columns are cut into equal chunks no longer
+                                than this                                        */
 } bubble_server_options;
 
 #define BUBBLE_SERVE_FIFO 0
