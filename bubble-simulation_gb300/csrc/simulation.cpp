@@ -52,16 +52,29 @@ int default_chunk(const uint32_t grid[3], int ty) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long tiles = (long)((grid[0] + 31) / 32) * (long)((grid[1] + ty - 1) / ty);
-    // Aim at >= 24 CTAs per SM over the launch (about a dozen waves of two
-    // resident CTAs, so the tail wave is short) while keeping chunks >= 32
-    // planes so each chunk's prologue stays a small share of its work.
-    // Measured (ms per step): 512^3 lz 128 13.07, 103 13.11, 64 13.20, 256
-    // 13.45; 256^3 lz 32 1.79, 16 1.84; 128^3 lz 32 0.281, 16 0.293, 64 0.388.
-    const long want = (long)sms * 24;
-    long chunks = (want + tiles - 1) / tiles;
-    if (chunks < 1) chunks = 1;
-    long lz = ((long)grid[2] + chunks - 1) / chunks;
-    if (lz < 32) lz = 32;
+    // Two regimes, measured (ms per step, 8 bubbles):
+    //  * lattices too small to fill the GPU with 16-plane chunks are latency
+    //    bound: fill one wave of two CTAs per SM with chunks of >= 8 planes
+    //    (48^3: lz 8 0.062, 16 0.105, 48 0.277; 64^3: 8 0.062, 16 0.105,
+    //    32 0.194; 96^3: 12 0.116, 16 0.146, 32 0.197);
+    //  * larger lattices: aim at >= 24 CTAs per SM over the launch (about a
+    //    dozen waves, so the tail wave is short) with chunks of >= 32 planes
+    //    so each chunk's prologue stays a small share of its work (128^3: 32
+    //    0.281, 16 0.293; 192^3: 48 0.776, 32 0.785, 16 0.816; 256^3: 32
+    //    1.750, 16 1.798; 512^3: 128 13.07, 64 13.20, 256 13.45).
+    const long resident = 2L * sms;
+    long lz;
+    if (tiles * (((long)grid[2] + 15) / 16) < resident) {
+        const long chunks = (resident + tiles - 1) / tiles;
+        lz = ((long)grid[2] + chunks - 1) / chunks;
+        if (lz < 8) lz = 8;
+    } else {
+        const long want = (long)sms * 24;
+        long chunks = (want + tiles - 1) / tiles;
+        if (chunks < 1) chunks = 1;
+        lz = ((long)grid[2] + chunks - 1) / chunks;
+        if (lz < 32) lz = 32;
+    }
     if (lz > (long)grid[2]) lz = grid[2];
     return (int)lz;
 }
