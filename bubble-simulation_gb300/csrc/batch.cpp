@@ -285,10 +285,19 @@ int Batch::add(const bubble_spec &spec, uint32_t *index, std::string &err) {
     L.schedule = make_schedule(spec.nucleation, spec.bubbles, d.seed_radius, L.grid, spec.nucleation_duration,
                                spec.seed);
     {
-        // equal chunks no longer than the cap
-        const int nz = (int)L.grid[2];
-        const int pieces = (nz + lz_cap_ - 1) / lz_cap_;
-        L.lz = (nz + pieces - 1) / pieces;
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const long tiles = (long)((L.grid[0] + 31) / 32) * (long)((L.grid[1] + ty_ - 1) / ty_);
+        L.solo = tiles * (((long)L.grid[2] + 31) / 32) >= 2L * std::max(sms, 1);
+        if (L.solo) {
+            L.lz = default_chunk(L.grid, ty_);
+        } else {
+            // equal chunks no longer than the cap
+            const int nz = (int)L.grid[2];
+            const int pieces = (nz + lz_cap_ - 1) / lz_cap_;
+            L.lz = (nz + pieces - 1) / pieces;
+        }
     }
     const int rc = allocate(L, err);
     if (rc != BUBBLE_OK) return rc;
@@ -319,7 +328,7 @@ int Batch::remove(uint32_t k, std::string &err) {
 void Batch::plan_items() {
     item_order_.clear();
     for (uint32_t k = 0; k < lats_.size(); ++k)
-        if (lats_[k].state) item_order_.push_back(k);
+        if (lats_[k].state && !lats_[k].solo) item_order_.push_back(k);
     std::stable_sort(item_order_.begin(), item_order_.end(),
                      [&](uint32_t a, uint32_t c) { return lats_[a].cells > lats_[c].cells; });
     n_items_ = 0;
@@ -360,11 +369,15 @@ int Batch::ensure_capacity(size_t n, std::string &err) {
 // trade the 5-plane prologue of every chunk against the tail of each
 // stage's round once the batch fills the GPU.  The lattices are still in
 // their quiescent initial state, an exact fixed point, so the timing steps
-// change nothing.
+// change nothing.  Solo lattices keep their plain-path chunk.
 int Batch::autotune(std::string &err) {
     std::vector<std::vector<int>> cands;
     std::vector<int> single;
     for (auto &L : lats_) {
+        if (L.solo) {  // runs alone with the plain path's chunk
+            single.push_back(L.lz);
+            continue;
+        }
         const int lz = autotune_chunk(L.grid, ty_, fast_, err);
         if (lz <= 0) return BUBBLE_ERR_CUDA;
         single.push_back(lz);
@@ -375,7 +388,7 @@ int Batch::autotune(std::string &err) {
         for (auto &L : lats_) {
             const int nz = (int)L.grid[2];
             const int pieces = (nz + cap - 1) / cap;
-            c.push_back((nz + pieces - 1) / pieces);
+            c.push_back(L.solo ? L.lz : (nz + pieces - 1) / pieces);
         }
         if (std::find(cands.begin(), cands.end(), c) == cands.end()) cands.push_back(c);
     }
@@ -530,8 +543,13 @@ int Batch::advance(uint64_t steps, std::string &err) {
         // the kernel numbers the grabs of a launch's rounds in 32 bits
         k = std::min<uint64_t>(
             k, std::max<uint64_t>(1, 0x7fffffffull / (3ull * (uint64_t)(std::max(n_items_, 1) + grid_))));
-        const int rc = launch_chunk(k, err);
+        int rc = launch_chunk(k, err);
         if (rc != BUBBLE_OK) return rc;
+        for (auto &L : lats_) {
+            if (!L.state || !L.solo) continue;
+            rc = launch_solo(L, k, err);
+            if (rc != BUBBLE_OK) return rc;
+        }
         for (auto &L : lats_) {
             if (!L.state) continue;
             L.cur = (uint32_t)((L.cur + k) % 3);
@@ -539,6 +557,38 @@ int Batch::advance(uint64_t steps, std::string &err) {
             L.steps += k;
         }
         done += k;
+    }
+    return BUBBLE_OK;
+}
+
+// k steps of one solo lattice: three stage launches per step, the slot
+// rotation of src/gpu/sim.rs:1046-1051, on the batch's stream after its
+// shared launch.
+int Batch::launch_solo(Lat &L, uint64_t k, std::string &err) {
+    for (uint64_t j = 0; j < k; ++j) {
+        const uint32_t cur = (uint32_t)((L.cur + j) % 3);
+        uint32_t in[3], out[3];
+        stage_slots(cur, in, out);
+        for (int st = 0; st < 3; ++st) {
+            StageArgs<float> A;
+            A.field_n = (const V2<float> *)L.field[cur];
+            A.fluid_n = (const V4<float> *)L.fluid[cur];
+            A.field_in = (const V2<float> *)L.field[in[st]];
+            A.fluid_in = (const V4<float> *)L.fluid[in[st]];
+            A.field_out = (V2<float> *)L.field[out[st]];
+            A.fluid_out = (V4<float> *)L.fluid[out[st]];
+            A.a0 = kRK3[st][0];
+            A.a1 = kRK3[st][1];
+            A.dt = L.dt;
+            A.stage = st;
+            const TileShape tile{32, ty_, L.lz};
+            const int tma = L.tma_ok ? 1 : 0;
+            const cudaError_t e =
+                fast_ ? launch::stage_v2_f32_fast(A, L.P, tile, 0, L.maps[in[st]], tma, d_status_, stream_)
+                      : launch::stage_v2_f32_strict(A, L.P, tile, 0, L.maps[in[st]], tma, d_status_, stream_);
+            BATCH_CUDA(e, "stage kernel of a solo lattice");
+            ++launches_;
+        }
     }
     return BUBBLE_OK;
 }

@@ -73,6 +73,10 @@ class Batch {
         uint64_t steps = 0;
         uint32_t cur = 0;
         int lz = 16;
+        // A lattice that fills the GPU by itself (two CTAs per SM with
+        // 32-plane chunks) gains nothing from the shared launch: it runs
+        // through the plain stage kernel with the plain path's chunk.
+        bool solo = false;
         uint64_t bytes = 0;
         std::vector<bubble_event> schedule;
         size_t next_event = 0;
@@ -83,6 +87,7 @@ class Batch {
     int nucleate_due(Lat &L, std::string &err);
     uint64_t steps_until_event(const Lat &L, uint64_t cap) const;
     int launch_chunk(uint64_t k, std::string &err);
+    int launch_solo(Lat &L, uint64_t k, std::string &err);
     int autotune(std::string &err);
     void plan_items();
     int ensure_capacity(size_t n, std::string &err);

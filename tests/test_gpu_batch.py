@@ -60,6 +60,33 @@ def test_batch_equals_plain_strict(bubble, gpu, events):
             assert times[k] == sim.time
 
 
+@pytest.mark.parametrize("math", ["strict", "fast"])
+def test_batch_solo_lattice_equals_plain(bubble, gpu, math):
+    """A lattice that fills the GPU by itself (here 192^3) runs solo through
+    the plain stage kernel with the plain path's chunk, beside the batched
+    small lattices: it equals the plain path bit for bit in both arithmetic
+    modes (same kernel, same chunk), events mid-run included."""
+    model = bubble.Model(eta=0.1, seed_kind="cells", seed_value=12.0)
+    big = bubble.SimulationSpec(model=model, grid=(192, 192, 192), nucleation="uniform", bubbles=4,
+                                nucleation_duration=2.0, seed=9, math=math)
+    specs = [big] + mixed_specs(bubble, 3, math, seed=5)
+    steps = 12
+    with bubble.Batch(specs) as b:
+        b.advance(5)
+        b.advance(steps - 5)
+        got = [b.copy_state(k) for k in range(len(specs))]
+        times = [b.time(k) for k in range(len(specs))]
+    (f, u), _ = plain_run(bubble, big, steps)
+    assert np.array_equal(got[0][0], f) and np.array_equal(got[0][1], u)
+    with bubble.Simulation(big) as sim:
+        sim.advance(steps)
+        assert times[0] == sim.time
+    if math == "strict":
+        for k, spec in enumerate(specs[1:], start=1):
+            (f, u), _ = plain_run(bubble, spec, steps)
+            assert np.array_equal(got[k][0], f) and np.array_equal(got[k][1], u), k
+
+
 def test_batch_fast_outcomes_match_plain(bubble, gpu):
     """The batched-ensemble workload in miniature: grow/collapse outcome of each
     run equals the plain path's, fields within 1e-4 after 300 steps."""
