@@ -625,7 +625,11 @@ BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2, const LatticeParams<R>
     FaceSide<R> s;
     R vx = q.x, vy = q.y, vz = q.z;
     const R p = q.w;
-    R v2raw = vx * vx + vy * vy + vz * vz;
+    // The fast forms round explicitly wherever the compiler could contract
+    // differently at the chunk prologue's and the z-march's call sites.
+    R v2raw;
+    if constexpr (FAST && sizeof(R) == 4) v2raw = dot3_rn(vx, vy, vz);
+    else v2raw = vx * vx + vy * vy + vz * vz;
     if constexpr (FAST) {
         // The velocity half of sanitise (shaders/step.wgsl:61-72): the fast
         // face states floor only the pressure and leave the velocity clamp to
@@ -636,7 +640,7 @@ BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2, const LatticeParams<R>
             vx = vx * sc;
             vy = vy * sc;
             vz = vz * sc;
-            v2raw = vx * vx + vy * vy + vz * vz;
+            v2raw = dot3_rn(vx, vy, vz);
         }
     }
     const R v2 = vmin(v2raw, zmax2);
@@ -688,10 +692,10 @@ BUBBLE_DEV FaceSide<R> face_side(const V4<R> &q, R zmax2, const LatticeParams<R>
         const R w = (R(4.0) * pf) * rcp_approx(om);
         {
             const float2 uzw = p_mul(bc2(w), make_float2(vy, vz));
-            s.u = V4<R>{PERT ? w * v2 + R(3.0) * p : w - p, w * vx, uzw.x, uzw.y};
+            s.u = V4<R>{PERT ? __fmaf_rn(w, v2, __fmul_rn(R(3.0), p)) : w - p, w * vx, uzw.x, uzw.y};
         }
-        const R inv_den = rcp_approx(R(1.0) - v2 * cs2);
-        const R tt = R(1.0) - (R(2.0) / R(3.0)) * (vd * vd) - cs2 * v2;
+        const R inv_den = rcp_approx(__fmaf_rn(-v2, cs2, R(1.0)));
+        const R tt = __fmaf_rn(-cs2, v2, __fmaf_rn(-(R(2.0) / R(3.0)), __fmul_rn(vd, vd), R(1.0)));
         const R rad = vmax(om * tt, R(0.0));
         const R cs = R(0.57735026918962576451);
         const R a = vd * ((R(2.0) / R(3.0)) * inv_den);
