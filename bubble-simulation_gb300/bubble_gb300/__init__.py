@@ -210,7 +210,7 @@ class Simulation:
         check(self._L.bubble_set_stream(self._h, stream_ptr))
 
     def set_path(self, path: str):
-        """"fused" (default), "reference" (primitives + stage passes) or "fused_sync"."""
+        """"fused" (default) or "reference" (primitives + stage passes)."""
         check(self._L.bubble_ext_set_path(self._h, _lib.PATHS[path]))
 
     def set_tile(self, ty: int, lz: int):

@@ -30,8 +30,7 @@ MATH = {"fast": 0, "strict": 1}
 EOS = {"bag": 0, "bag_dof": 1, "gamma_law": 2, "thermal": 3}
 PATH_FUSED = 0
 PATH_REFERENCE = 1
-PATH_FUSED_SYNC = 2
-PATHS = {"fused": PATH_FUSED, "reference": PATH_REFERENCE, "fused_sync": PATH_FUSED_SYNC}
+PATHS = {"fused": PATH_FUSED, "reference": PATH_REFERENCE}
 MIN_GRID = 8
 MAX_GRID = 2048
 MAX_BATCH = 1024
@@ -189,7 +188,9 @@ SIGNATURES = [
     ("bubble_ext_stream", _P, [_P]),
     ("bubble_ext_launches", ctypes.c_uint64, [_P]),
     ("bubble_ext_inject_allocation_failure", None, []),
-    ("bubble_diagnostics_noalloc", ctypes.c_int, [_P, _P, _U32P, ctypes.POINTER(Model), ctypes.c_int32, _P, _P]),
+    ("bubble_ext_test_expire_stage_wait", ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_int32]),
+    ("bubble_ext_test_expire_batch_barrier", ctypes.c_int, [_P, ctypes.c_int32]),
+    ("bubble_diagnostics_noalloc", ctypes.c_int, [_P, _P, ctypes.POINTER(Spec), _P, _P]),
     # bubble_batch.h
     ("bubble_batch_options_default", None, [ctypes.POINTER(BatchOptions)]),
     ("bubble_batch_create", ctypes.c_int, [ctypes.POINTER(Spec), ctypes.c_uint32, ctypes.POINTER(BatchOptions),

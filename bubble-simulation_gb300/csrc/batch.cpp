@@ -488,9 +488,18 @@ int Batch::launch_chunk(uint64_t k, std::string &err) {
         if (e == cudaSuccess) e = cudaMemsetAsync(d_counters_, 0, 16, stream_);
         if (e == cudaSuccess)
             e = launch::batch_launch(fast_, ty_, d_lat_, n_lat, n_items_, (int)k, d_counters_, d_status_, grid_,
+                                     test_barrier_shift_ ? 1u : 0u, test_barrier_shift_ ? test_barrier_shift_ : 32,
                                      stream_);
         return e;
     };
+    if (test_barrier_shift_) {
+        // test hook: one direct launch whose grid barrier no arrival releases
+        const cudaError_t e = enqueue();
+        test_barrier_shift_ = 0;
+        BATCH_CUDA(e, "batch launch");
+        ++launches_;
+        return BUBBLE_OK;
+    }
     if (use_graph_) {
         const auto key = std::make_tuple(k, n_lat, n_items_, grid_);
         if (!graph_ok_ || graph_key_ != key) {

@@ -17,8 +17,11 @@
 namespace bubble {
 namespace dev {
 
-// Bounded grid barrier for a cooperative launch.  Returns false on expiry.
-BUBBLE_DEV bool grid_barrier(unsigned int *count, unsigned int *gen, int *status) {
+// Bounded grid barrier for a cooperative launch: the last of gridDim.x +
+// `extra` arrivals releases it (extra is 0 except in the test hook
+// bubble_ext_test_expire_batch_barrier, where no arrival is the last); a CTA
+// waits at most 2^shift SM cycles.  Returns false on expiry.
+BUBBLE_DEV bool grid_barrier(unsigned int *count, unsigned int *gen, int *status, unsigned int extra, int shift) {
     __shared__ int ok_s;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -30,14 +33,14 @@ BUBBLE_DEV bool grid_barrier(unsigned int *count, unsigned int *gen, int *status
         __threadfence();
         const unsigned int arrived = atomicAdd(count, 1u) + 1u;
         int ok = 1;
-        if (arrived == gridDim.x) {
+        if (arrived == gridDim.x + extra) {
             atomicExch(count, 0u);
             __threadfence();
             atomicAdd(gen, 1u);
         } else {
             const long long t0 = clock64();
             while (*vgen == g) {
-                if (clock64() - t0 > (1ll << 32)) {
+                if (clock64() - t0 > (1ll << shift)) {
                     ok = 0;
                     atomicOr(status, 2);
                     break;
@@ -58,7 +61,7 @@ BUBBLE_DEV bool grid_barrier(unsigned int *count, unsigned int *gen, int *status
 template <bool FAST, int TY>
 __global__ void __launch_bounds__(V2Layout<float, TY>::NT, V2Layout<float, TY>::MIN_BLOCKS)
     batch_v2_kernel(const BatchLattice *__restrict__ lat, int n_lat, int n_items, int steps,
-                    unsigned int *counters, int *status) {
+                    unsigned int *counters, int *status, unsigned int barrier_extra, int barrier_shift) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int item_s;
     unsigned int round = 0;
@@ -115,7 +118,7 @@ __global__ void __launch_bounds__(V2Layout<float, TY>::NT, V2Layout<float, TY>::
                     return;
                 }
             }
-            if (!grid_barrier(&counters[0], &counters[1], status)) return;
+            if (!grid_barrier(&counters[0], &counters[1], status, barrier_extra, barrier_shift)) return;
         }
     }
 }

@@ -96,8 +96,13 @@ class Batch {
    public:
     // z planes per work item of lattices that join later (0: 64)
     void set_chunk_planes(int planes) { lz_cap_ = planes > 0 ? planes : 64; }
+    // Test hook: the next persistent launch runs its grid barrier with a
+    // release count no arrival reaches and a 2^shift-cycle wait limit, so
+    // every CTA's barrier wait expires and sets bit 1 of the status word.
+    void arm_barrier_expiry(int shift) { test_barrier_shift_ = shift; }
 
    private:
+    int test_barrier_shift_ = 0;  // 0: off
 
     std::vector<Lat> lats_;
     std::vector<uint32_t> item_order_;  // active lattices by decreasing size

@@ -287,9 +287,16 @@ int bubble_load_state_f64(bubble_sim *sim, const double *field, const double *fl
 // ---------------------------------------------------------------------------
 int bubble_ext_set_path(bubble_sim *sim, int32_t path) {
     if (!sim || !sim->impl) return fail(BUBBLE_ERR_INVALID, "sim is NULL");
-    if (path != BUBBLE_PATH_FUSED && path != BUBBLE_PATH_REFERENCE && path != BUBBLE_PATH_FUSED_SYNC)
+    if (path != BUBBLE_PATH_FUSED && path != BUBBLE_PATH_REFERENCE)
         return fail(BUBBLE_ERR_INVALID, "unknown kernel path");
     sim->impl->set_path(static_cast<bubble::KernelPath>(path));
+    return BUBBLE_OK;
+}
+int bubble_ext_test_expire_stage_wait(bubble_sim *sim, uint32_t extra_bytes, int32_t wait_shift) {
+    if (!sim || !sim->impl) return fail(BUBBLE_ERR_INVALID, "sim is NULL");
+    if (extra_bytes < 1 || extra_bytes > 65536) return fail(BUBBLE_ERR_INVALID, "extra_bytes must be 1..65536");
+    if (wait_shift < 10 || wait_shift > 31) return fail(BUBBLE_ERR_INVALID, "wait_shift must be 10..31");
+    sim->impl->arm_wait_expiry(extra_bytes, wait_shift);
     return BUBBLE_OK;
 }
 int bubble_ext_set_tile(bubble_sim *sim, int32_t ty, int32_t lz) {

@@ -72,6 +72,13 @@ float bubble_batch_time(const bubble_batch *batch, uint32_t index) {
     return batch->impl->time(index);
 }
 
+int bubble_ext_test_expire_batch_barrier(bubble_batch *batch, int32_t wait_shift) {
+    if (!batch || !batch->impl) return fail(BUBBLE_ERR_INVALID, "batch is NULL");
+    if (wait_shift < 10 || wait_shift > 32) return fail(BUBBLE_ERR_INVALID, "wait_shift must be 10..32");
+    batch->impl->arm_barrier_expiry(wait_shift);
+    return BUBBLE_OK;
+}
+
 int bubble_autotune_chunk(const uint32_t grid[3], int32_t tile_y, int32_t math, int32_t *lz_out) {
     if (!grid || !lz_out) return fail(BUBBLE_ERR_INVALID, "grid and lz_out must be non-NULL");
     std::string err;

@@ -55,18 +55,22 @@ struct Header {
     uint32_t reserved;
 };
 
-uint32_t crc32_of(const unsigned char *p, size_t n, uint32_t crc = 0xFFFFFFFFu) {
-    static uint32_t table[256];
-    static bool ready = false;
-    if (!ready) {
+// CRC-32 (reflected polynomial 0xEDB88320) lookup table, built at compile time
+// so concurrent saves and loads share it without any initialisation race.
+struct Crc32Table {
+    uint32_t t[256];
+    constexpr Crc32Table() : t() {
         for (uint32_t i = 0; i < 256; ++i) {
             uint32_t c = i;
             for (int k = 0; k < 8; ++k) c = (c & 1u) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
-            table[i] = c;
+            t[i] = c;
         }
-        ready = true;
     }
-    for (size_t i = 0; i < n; ++i) crc = table[(crc ^ p[i]) & 0xFFu] ^ (crc >> 8);
+};
+constexpr Crc32Table kCrc32Table{};
+
+uint32_t crc32_of(const unsigned char *p, size_t n, uint32_t crc = 0xFFFFFFFFu) {
+    for (size_t i = 0; i < n; ++i) crc = kCrc32Table.t[(crc ^ p[i]) & 0xFFu] ^ (crc >> 8);
     return crc;
 }
 

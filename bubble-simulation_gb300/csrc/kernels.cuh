@@ -4,8 +4,6 @@
 //   nucleate_kernel      shaders/nucleate.wgsl:59-85
 //   prim_kernel          shaders/primitives.wgsl:16-23   (reference-structured path)
 //   stage_ref_kernel     shaders/step.wgsl:92-174         (reference-structured path)
-//   stage_fused_kernel   shaders/primitives.wgsl + step.wgsl fused: one launch per
-//                        RK stage, con2prim on staged planes, each face flux once
 //   diag_kernel          shaders/reduce.wgsl:49-140, single pass, FP64 sums
 //
 // This header is included by translation units that differ only in their
@@ -228,271 +226,6 @@ __global__ void stage_ref_kernel(StageArgs<R> A, const V4<R> *__restrict__ prim,
         A.field_out[i0] = V2<R>{A.a0 * fn.x + A.a1 * fu.x, A.a0 * fn.y + A.a1 * fu.y};
         A.fluid_out[i0] = V4<R>{A.a0 * un.x + A.a1 * uu.x, A.a0 * un.y + A.a1 * uu.y,
                                 A.a0 * un.z + A.a1 * uu.z, A.a0 * un.w + A.a1 * uu.w};
-    }
-}
-
-// ---------------------------------------------------------------------------
-//  Fused stage kernel
-// ---------------------------------------------------------------------------
-// A CTA owns a TX x TY column of cells and marches it through a chunk of LZ
-// z-planes.  Per plane z it
-//   A  stages plane z+2 (x/y halo of 2, corners skipped) from HBM, recovers
-//      primitives once per cell and keeps them, sanitised, in a 4-plane ring;
-//      phi goes to an 8-plane ring;
-//   B1 computes, once per cell and axis, the limited slope and the two
-//      sanitised face states q -+ s/2 (x and y for plane z, z for plane z+1);
-//   B2 computes every face flux once: x and y faces of plane z and the z face
-//      z+1/2 (the z face z-1/2 is kept from the previous plane);
-//   C  forms the 7-point Laplacian, central gradient, friction source and
-//      the RK stage combine for plane z and writes U_out.
-// The work items of each phase are laid out so every warp takes one kind of
-// item (the counts that precede each kind are multiples of 32).
-template <typename R, int TX, int TY>
-struct FusedLayout {
-    static constexpr int NT = TX * (TY + 1);
-    static constexpr int PW = TX + 4;
-    static constexpr int PH = TY + 4;
-    static constexpr int PC = PW * PH;
-    static constexpr int NC = TX * TY;
-    static constexpr int PRIM_RING = 4;
-    static constexpr int PHI_RING = 8;
-    // offsets in bytes
-    static constexpr size_t o_prim = 0;
-    static constexpr size_t o_xlo = o_prim + sizeof(V4<R>) * PRIM_RING * PC;
-    static constexpr size_t o_xhi = o_xlo + sizeof(V4<R>) * TY * (TX + 2);
-    static constexpr size_t o_ylo = o_xhi + sizeof(V4<R>) * TY * (TX + 2);
-    static constexpr size_t o_yhi = o_ylo + sizeof(V4<R>) * (TY + 2) * TX;
-    static constexpr size_t o_zlo = o_yhi + sizeof(V4<R>) * (TY + 2) * TX;
-    static constexpr size_t o_zhi = o_zlo + sizeof(V4<R>) * NC;
-    static constexpr size_t o_fx = o_zhi + sizeof(V4<R>) * 2 * NC;
-    static constexpr size_t o_fy = o_fx + sizeof(V4<R>) * TY * (TX + 1);
-    static constexpr size_t o_fz = o_fy + sizeof(V4<R>) * (TY + 1) * TX;
-    static constexpr size_t o_phi = o_fz + sizeof(V4<R>) * 2 * NC;
-    static constexpr size_t bytes = o_phi + sizeof(R) * PHI_RING * PC;
-};
-
-template <typename R, bool FAST, int MIXED, int TX, int TY>
-__global__ void __launch_bounds__(TX *(TY + 1))
-    stage_fused_kernel(StageArgs<R> A, LatticeParams<R> P, int lz) {
-    using L = FusedLayout<R, TX, TY>;
-    constexpr int NT = L::NT, PW = L::PW, PC = L::PC, NC = L::NC;
-    extern __shared__ __align__(128) unsigned char smem[];
-    V4<R> *prim_s = reinterpret_cast<V4<R> *>(smem + L::o_prim);
-    V4<R> *xlo = reinterpret_cast<V4<R> *>(smem + L::o_xlo);
-    V4<R> *xhi = reinterpret_cast<V4<R> *>(smem + L::o_xhi);
-    V4<R> *ylo = reinterpret_cast<V4<R> *>(smem + L::o_ylo);
-    V4<R> *yhi = reinterpret_cast<V4<R> *>(smem + L::o_yhi);
-    V4<R> *zlo = reinterpret_cast<V4<R> *>(smem + L::o_zlo);
-    V4<R> *zhi = reinterpret_cast<V4<R> *>(smem + L::o_zhi);
-    V4<R> *fxs = reinterpret_cast<V4<R> *>(smem + L::o_fx);
-    V4<R> *fys = reinterpret_cast<V4<R> *>(smem + L::o_fy);
-    V4<R> *fzs = reinterpret_cast<V4<R> *>(smem + L::o_fz);
-    R *phi_s = reinterpret_cast<R *>(smem + L::o_phi);
-
-    const int t = threadIdx.x;
-    const int ntx = (P.nx + TX - 1) / TX;
-    const int x0 = (blockIdx.x % ntx) * TX;
-    const int y0 = (blockIdx.x / ntx) * TY;
-    const int z0 = blockIdx.y * lz;
-    const int z1 = min(z0 + lz, P.nz);
-    const int xe = min(TX, P.nx - x0);  // valid cells in this tile
-    const int ye = min(TY, P.ny - y0);
-    const R zmax2 = P.z_max * P.z_max;
-    const size_t plane = (size_t)P.nx * (size_t)P.ny;
-
-    // ---- A: stage plane p (any integer in [z0-2, z1+1]) -------------------
-    auto stage_plane = [&](int p) {
-        const int gz = wrap1(p, P.nz);
-        const size_t base = (size_t)gz * plane;
-        V4<R> *pr = prim_s + ((p + 8) & (L::PRIM_RING - 1)) * PC;
-        R *ph = phi_s + ((p + 8) & (L::PHI_RING - 1)) * PC;
-        constexpr int band = TY * PW;  // rows 2..TY+1, all columns
-        constexpr int total = band + 4 * TX;
-        for (int k = t; k < total; k += NT) {
-            int i, j;
-            if (k < band) {
-                j = 2 + k / PW;
-                i = k - (j - 2) * PW;
-            } else {
-                const int kk = k - band;
-                const int r = kk / TX;
-                j = r < 2 ? r : TY + r;
-                i = 2 + (kk - r * TX);
-            }
-            if (i >= xe + 4 || j >= ye + 4) continue;
-            const int gx = wrap1(x0 - 2 + i, P.nx);
-            const int gy = wrap1(y0 - 2 + j, P.ny);
-            const size_t g = base + (size_t)gy * P.nx + gx;
-            const V4<R> u = A.fluid_in[g];
-            const R phi = A.field_in[g].x;
-            pr[j * PW + i] = sanitise(recover<R, FAST, MIXED>(u, P), P.p_floor, zmax2);
-            ph[j * PW + i] = phi;
-        }
-    };
-    auto prim_at = [&](int p, int c) -> const V4<R> & {
-        return prim_s[((p + 8) & (L::PRIM_RING - 1)) * PC + c];
-    };
-    // z face states of cell p for column n (centre index c in the plane).
-    auto z_states = [&](int p, int n, V4<R> &lo, V4<R> &hi) {
-        const int i = n % TX, j = n / TX;
-        const int c = (j + 2) * PW + (i + 2);
-        const V4<R> q = prim_at(p, c);
-        const V4<R> s = limit_slope4(v4_sub(q, prim_at(p - 1, c)), v4_sub(prim_at(p + 1, c), q));
-        lo = sanitise(half_step(q, s, R(-1)), P.p_floor, zmax2);
-        hi = sanitise(half_step(q, s, R(1)), P.p_floor, zmax2);
-    };
-
-    // ---- warm-up: planes z0-2 .. z0+1, z face z0 - 1/2 ---------------------
-    for (int p = z0 - 2; p <= z0 + 1; ++p) stage_plane(p);
-    __syncthreads();
-    for (int n = t; n < NC; n += NT) {
-        V4<R> lo_m, hi_m, lo_0, hi_0;
-        z_states(z0 - 1, n, lo_m, hi_m);
-        z_states(z0, n, lo_0, hi_0);
-        zhi[((z0 + 8) & 1) * NC + n] = hi_0;
-        fzs[((z0 - 1 + 8) & 1) * NC + n] = hll_flux<2, R, FAST, MIXED>(hi_m, lo_0, zmax2, P);
-    }
-    // (the first loop iteration's barrier orders these writes)
-
-    for (int z = z0; z < z1; ++z) {
-        stage_plane(z + 2);
-        __syncthreads();
-        // ---- B1: face states --------------------------------------------
-        {
-            constexpr int n_z = NC;
-            constexpr int n_y = TX * (TY + 2);
-            constexpr int n_x = (TX + 2) * TY;
-            const int pz = z;
-            for (int k = t; k < n_z + n_y + n_x; k += NT) {
-                if (k < n_z) {
-                    V4<R> lo, hi;
-                    z_states(z + 1, k, lo, hi);
-                    zlo[k] = lo;
-                    zhi[((z + 1 + 8) & 1) * NC + k] = hi;
-                } else if (k < n_z + n_y) {
-                    const int kk = k - n_z;
-                    const int jj = kk / TX;  // cell row jj-1
-                    const int i = kk - jj * TX;
-                    const int c = (jj + 1) * PW + (i + 2);
-                    const V4<R> q = prim_at(pz, c);
-                    const V4<R> s =
-                        limit_slope4(v4_sub(q, prim_at(pz, c - PW)), v4_sub(prim_at(pz, c + PW), q));
-                    ylo[jj * TX + i] = sanitise(half_step(q, s, R(-1)), P.p_floor, zmax2);
-                    yhi[jj * TX + i] = sanitise(half_step(q, s, R(1)), P.p_floor, zmax2);
-                } else {
-                    const int kk = k - n_z - n_y;
-                    const int j = kk / (TX + 2);
-                    const int ii = kk - j * (TX + 2);  // cell column ii-1
-                    const int c = (j + 2) * PW + (ii + 1);
-                    const V4<R> q = prim_at(pz, c);
-                    const V4<R> s =
-                        limit_slope4(v4_sub(q, prim_at(pz, c - 1)), v4_sub(prim_at(pz, c + 1), q));
-                    xlo[j * (TX + 2) + ii] = sanitise(half_step(q, s, R(-1)), P.p_floor, zmax2);
-                    xhi[j * (TX + 2) + ii] = sanitise(half_step(q, s, R(1)), P.p_floor, zmax2);
-                }
-            }
-        }
-        __syncthreads();
-        // ---- B2: face fluxes ----------------------------------------------
-        {
-            constexpr int n_z = NC;
-            constexpr int n_y = TX * (TY + 1);
-            constexpr int n_x = (TX + 1) * TY;
-            for (int k = t; k < n_z + n_y + n_x; k += NT) {
-                if (k < n_z) {
-                    fzs[((z + 8) & 1) * NC + k] =
-                        hll_flux<2, R, FAST, MIXED>(zhi[((z + 8) & 1) * NC + k], zlo[k], zmax2, P);
-                } else if (k < n_z + n_y) {
-                    const int kk = k - n_z;
-                    const int f = kk / TX;  // face between rows f-1 and f
-                    const int i = kk - f * TX;
-                    fys[f * TX + i] = hll_flux<1, R, FAST, MIXED>(yhi[f * TX + i], ylo[(f + 1) * TX + i], zmax2, P);
-                } else {
-                    const int kk = k - n_z - n_y;
-                    const int j = kk / (TX + 1);
-                    const int f = kk - j * (TX + 1);  // face between columns f-1 and f
-                    fxs[j * (TX + 1) + f] =
-                        hll_flux<0, R, FAST, MIXED>(xhi[j * (TX + 2) + f], xlo[j * (TX + 2) + f + 1], zmax2, P);
-                }
-            }
-        }
-        __syncthreads();
-        // ---- C: sources and stage combine ---------------------------------
-        if (t < NC) {
-            const int i = t % TX, j = t / TX;
-            if (i < xe && j < ye) {
-                const int c = (j + 2) * PW + (i + 2);
-                const R *ph0 = phi_s + ((z + 8) & (L::PHI_RING - 1)) * PC;
-                const R *phm = phi_s + ((z - 1 + 8) & (L::PHI_RING - 1)) * PC;
-                const R *php = phi_s + ((z + 1 + 8) & (L::PHI_RING - 1)) * PC;
-                const size_t g = (size_t)z * plane + (size_t)(y0 + j) * P.nx + (x0 + i);
-                const V2<R> f0 = A.field_in[g];
-                const V4<R> u_in = A.fluid_in[g];
-                const R phi0 = f0.x, pi0 = f0.y;
-                const V4<R> q0 = prim_at(z, c);
-                R lap_sum = R(0);
-                R gx, gy, gz;
-                {
-                    const R m = ph0[c - 1], p = ph0[c + 1];
-                    lap_sum = lap_sum + (m + p - R(2.0) * phi0);
-                    gx = R(0.5) * (p - m) * P.inv_dx;
-                }
-                {
-                    const R m = ph0[c - PW], p = ph0[c + PW];
-                    lap_sum = lap_sum + (m + p - R(2.0) * phi0);
-                    gy = R(0.5) * (p - m) * P.inv_dx;
-                }
-                {
-                    const R m = phm[c], p = php[c];
-                    lap_sum = lap_sum + (m + p - R(2.0) * phi0);
-                    gz = R(0.5) * (p - m) * P.inv_dx;
-                }
-                const V4<R> fxm = fxs[j * (TX + 1) + i], fxp = fxs[j * (TX + 1) + i + 1];
-                const V4<R> fym = fys[j * TX + i], fyp = fys[(j + 1) * TX + i];
-                const V4<R> fzm = fzs[((z - 1 + 8) & 1) * NC + t], fzp = fzs[((z + 8) & 1) * NC + t];
-                V4<R> fd{R(0), R(0), R(0), R(0)};
-                fd.x = fd.x + (fxp.x - fxm.x) * P.inv_dx;
-                fd.y = fd.y + (fxp.y - fxm.y) * P.inv_dx;
-                fd.z = fd.z + (fxp.z - fxm.z) * P.inv_dx;
-                fd.w = fd.w + (fxp.w - fxm.w) * P.inv_dx;
-                fd.x = fd.x + (fyp.x - fym.x) * P.inv_dx;
-                fd.y = fd.y + (fyp.y - fym.y) * P.inv_dx;
-                fd.z = fd.z + (fyp.z - fym.z) * P.inv_dx;
-                fd.w = fd.w + (fyp.w - fym.w) * P.inv_dx;
-                fd.x = fd.x + (fzp.x - fzm.x) * P.inv_dx;
-                fd.y = fd.y + (fzp.y - fzm.y) * P.inv_dx;
-                fd.z = fd.z + (fzp.z - fzm.z) * P.inv_dx;
-                fd.w = fd.w + (fzp.w - fzm.w) * P.inv_dx;
-                const R laplacian = lap_sum * P.inv_dx * P.inv_dx;
-                const R vv = q0.x * q0.x + q0.y * q0.y + q0.z * q0.z;
-                R gam;
-                if constexpr (FAST) gam = rsqrt_approx(vmax(R(1.0) - vv, R(1e-12)));
-                else gam = R(1.0) / sqrt(vmax(R(1.0) - vv, R(1e-12)));
-                const R dphi_proper = gam * (pi0 + (q0.x * gx + q0.y * gy + q0.z * gz));
-                const R drag = P.eta * dphi_proper;
-                const R d_pi = laplacian - dpotential(phi0, P) - drag;
-                const R dE = -fd.x + drag * pi0;
-                const R dZx = -fd.y - drag * gx;
-                const R dZy = -fd.z - drag * gy;
-                const R dZz = -fd.w - drag * gz;
-                const V2<R> fu{f0.x + A.dt * pi0, f0.y + A.dt * d_pi};
-                const V4<R> uu{u_in.x + A.dt * dE, u_in.y + A.dt * dZx, u_in.z + A.dt * dZy,
-                               u_in.w + A.dt * dZz};
-                if (A.stage == 0) {
-                    A.field_out[g] = V2<R>{A.a1 * fu.x, A.a1 * fu.y};
-                    A.fluid_out[g] = V4<R>{A.a1 * uu.x, A.a1 * uu.y, A.a1 * uu.z, A.a1 * uu.w};
-                } else {
-                    const V2<R> fn = A.field_n[g];
-                    const V4<R> un = A.fluid_n[g];
-                    A.field_out[g] = V2<R>{rk_combine<R, FAST>(A.a0, A.a1, fn.x, fu.x),
-                                           rk_combine<R, FAST>(A.a0, A.a1, fn.y, fu.y)};
-                    A.fluid_out[g] = V4<R>{rk_combine<R, FAST>(A.a0, A.a1, un.x, uu.x),
-                                           rk_combine<R, FAST>(A.a0, A.a1, un.y, uu.y),
-                                           rk_combine<R, FAST>(A.a0, A.a1, un.z, uu.z),
-                                           rk_combine<R, FAST>(A.a0, A.a1, un.w, uu.w)};
-                }
-            }
-        }
     }
 }
 

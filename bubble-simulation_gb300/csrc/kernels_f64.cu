@@ -24,11 +24,6 @@ cudaError_t stage_ref_f64(const StageArgs<double> &A, const V4<double> *p,
                           const LatticeParams<double> &P, cudaStream_t s) {
     return stage_ref<double>(A, p, P, s);
 }
-cudaError_t stage_fused_f64(const StageArgs<double> &A, const LatticeParams<double> &P,
-                            TileShape shape, cudaStream_t s) {
-    if (shape.tx != 32 || shape.ty != 4) return cudaErrorInvalidValue;
-    return stage_fused<double, false, false, 4>(A, P, shape.lz, s);
-}
 cudaError_t diag_f64(const V2<double> *field, const V4<double> *fluid,
                      const LatticeParams<double> &P, void *partials, unsigned int *ticket,
                      DiagResult *out, cudaStream_t s) {

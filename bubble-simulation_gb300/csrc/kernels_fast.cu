@@ -5,28 +5,6 @@
 namespace bubble {
 namespace launch {
 
-using namespace launch_detail;
-
-cudaError_t stage_fused_f32_fast(const StageArgs<float> &A, const LatticeParams<float> &P,
-                                 TileShape shape, bool mixed, cudaStream_t s) {
-    if (shape.tx != 32) return cudaErrorInvalidValue;
-    if (shape.ty == 8) {
-        if (mixed) return stage_fused<float, true, true, 8>(A, P, shape.lz, s);
-        return stage_fused<float, true, false, 8>(A, P, shape.lz, s);
-    }
-    if (shape.ty == 4) {
-        if (mixed) return stage_fused<float, true, true, 4>(A, P, shape.lz, s);
-        return stage_fused<float, true, false, 4>(A, P, shape.lz, s);
-    }
-    return cudaErrorInvalidValue;
-}
-
-}  // namespace launch
-}  // namespace bubble
-
-namespace bubble {
-namespace launch {
-
 cudaError_t stage_v2_f32_fast(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
                               int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
     using namespace launch_detail;
@@ -62,10 +40,17 @@ size_t batch_smem_bytes(int ty) {
     return ty == 4 ? dev::V2Layout<float, 4>::bytes : dev::V2Layout<float, 8>::bytes;
 }
 cudaError_t batch_launch(bool fast, int ty, const void *lat, int n_lat, int n_items, int steps,
-                         unsigned int *counters, int *status, int grid, cudaStream_t s) {
-    if (!fast) return batch_launch_strict(ty, lat, n_lat, n_items, steps, counters, status, grid, s);
-    if (ty == 8) return launch_detail::batch_launch<true, 8>(lat, n_lat, n_items, steps, counters, status, grid, s);
-    if (ty == 4) return launch_detail::batch_launch<true, 4>(lat, n_lat, n_items, steps, counters, status, grid, s);
+                         unsigned int *counters, int *status, int grid, unsigned int barrier_extra,
+                         int barrier_shift, cudaStream_t s) {
+    if (!fast)
+        return batch_launch_strict(ty, lat, n_lat, n_items, steps, counters, status, grid, barrier_extra,
+                                   barrier_shift, s);
+    if (ty == 8)
+        return launch_detail::batch_launch<true, 8>(lat, n_lat, n_items, steps, counters, status, grid,
+                                                    barrier_extra, barrier_shift, s);
+    if (ty == 4)
+        return launch_detail::batch_launch<true, 4>(lat, n_lat, n_items, steps, counters, status, grid,
+                                                    barrier_extra, barrier_shift, s);
     return cudaErrorInvalidValue;
 }
 

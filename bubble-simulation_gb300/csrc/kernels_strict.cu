@@ -26,12 +26,6 @@ cudaError_t stage_ref_f32(const StageArgs<float> &A, const V4<float> *p,
                           const LatticeParams<float> &P, cudaStream_t s) {
     return stage_ref<float>(A, p, P, s);
 }
-cudaError_t stage_fused_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P,
-                                   TileShape shape, bool mixed, cudaStream_t s) {
-    if (shape.tx != 32 || shape.ty != 8) return cudaErrorInvalidValue;
-    if (mixed) return stage_fused<float, false, true, 8>(A, P, shape.lz, s);
-    return stage_fused<float, false, false, 8>(A, P, shape.lz, s);
-}
 cudaError_t diag_f32(const V2<float> *field, const V4<float> *fluid,
                      const LatticeParams<float> &P, int mode, void *partials,
                      unsigned int *ticket, DiagResult *out, cudaStream_t s) {
@@ -44,15 +38,6 @@ cudaError_t diag_f32(const V2<float> *field, const V4<float> *fluid,
 
 size_t diag_partials_bytes() { return sizeof(dev::DiagPartial) * dev::kDiagMaxBlocks; }
 int diag_blocks_for(uint64_t cells) { return dev::diag_blocks(cells); }
-
-bool fused_shape_supported(int precision_double, int ty) {
-    return precision_double ? ty == 4 : (ty == 4 || ty == 8);
-}
-size_t fused_smem_bytes(int precision_double, int ty) {
-    if (precision_double) return dev::FusedLayout<double, 32, 4>::bytes;
-    return ty == 4 ? dev::FusedLayout<float, 32, 4>::bytes : dev::FusedLayout<float, 32, 8>::bytes;
-}
-int fused_threads(int ty) { return 32 * (ty + 1); }
 
 }  // namespace launch
 }  // namespace bubble
@@ -90,9 +75,11 @@ int batch_max_grid_strict(int ty) {
     return launch_detail::batch_max_grid<false, 8>();
 }
 cudaError_t batch_launch_strict(int ty, const void *lat, int n_lat, int n_items, int steps,
-                                unsigned int *counters, int *status, int grid, cudaStream_t s) {
+                                unsigned int *counters, int *status, int grid, unsigned int barrier_extra,
+                                int barrier_shift, cudaStream_t s) {
     if (ty != 8) return cudaErrorInvalidValue;
-    return launch_detail::batch_launch<false, 8>(lat, n_lat, n_items, steps, counters, status, grid, s);
+    return launch_detail::batch_launch<false, 8>(lat, n_lat, n_items, steps, counters, status, grid, barrier_extra,
+                                                 barrier_shift, s);
 }
 
 }  // namespace launch

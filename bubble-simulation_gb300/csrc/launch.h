@@ -16,14 +16,6 @@
 namespace bubble {
 namespace launch {
 
-// Tile shapes compiled for the fused stage kernel (x is always 32 cells).
-// `ty` selects the instantiation; `lz` is a runtime choice.
-bool fused_shape_supported(int precision_double, int ty);
-// Dynamic shared memory of one CTA of the fused kernel.
-size_t fused_smem_bytes(int precision_double, int ty);
-// Threads per CTA of the fused kernel.
-int fused_threads(int ty);
-
 // ---- FP32 (strict translation unit: no FMA contraction) ----------------
 cudaError_t init_f32(V2<float> *field, V4<float> *fluid, uint64_t n, float e_ref,
                      cudaStream_t s);
@@ -34,17 +26,12 @@ cudaError_t prim_f32(const V4<float> *fluid, V4<float> *prim, uint64_t n,
                      const LatticeParams<float> &P, cudaStream_t s);
 cudaError_t stage_ref_f32(const StageArgs<float> &A, const V4<float> *prim,
                           const LatticeParams<float> &P, cudaStream_t s);
-cudaError_t stage_fused_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P,
-                                   TileShape shape, bool mixed, cudaStream_t s);
+
 // `mode`: 0 plain, 1 mixed, 2 perturbation form, 3 gamma-law equation of
 // state, 4 thermal potential (physics.cuh kPlain/kMixed/kPert/kGamma/kThermal).
 cudaError_t diag_f32(const V2<float> *field, const V4<float> *fluid,
                      const LatticeParams<float> &P, int mode, void *partials,
                      unsigned int *ticket, DiagResult *out, cudaStream_t s);
-
-// ---- FP32 (fast translation unit: FMA, approximate rcp/sqrt) ------------
-cudaError_t stage_fused_f32_fast(const StageArgs<float> &A, const LatticeParams<float> &P,
-                                 TileShape shape, bool mixed, cudaStream_t s);
 
 // ---- FP64 (the FP64 CUDA oracle; no FMA contraction) --------------------
 cudaError_t init_f64(V2<double> *field, V4<double> *fluid, uint64_t n, double e_ref,
@@ -55,8 +42,6 @@ cudaError_t prim_f64(const V4<double> *fluid, V4<double> *prim, uint64_t n,
                      const LatticeParams<double> &P, cudaStream_t s);
 cudaError_t stage_ref_f64(const StageArgs<double> &A, const V4<double> *prim,
                           const LatticeParams<double> &P, cudaStream_t s);
-cudaError_t stage_fused_f64(const StageArgs<double> &A, const LatticeParams<double> &P,
-                            TileShape shape, cudaStream_t s);
 cudaError_t diag_f64(const V2<double> *field, const V4<double> *fluid,
                      const LatticeParams<double> &P, void *partials, unsigned int *ticket,
                      DiagResult *out, cudaStream_t s);
@@ -88,11 +73,16 @@ namespace launch {
 // ---- batched persistent launch (batch.cuh) ---------------------------------
 // lat: device array of BatchLattice; counters: 3 zeroed uint32 (barrier
 // count, barrier generation, work counter).  Cooperative launch with `grid`
-// CTAs, which must not exceed batch_max_grid(fast, ty).
+// CTAs, which must not exceed batch_max_grid(fast, ty).  The grid barrier
+// between stages releases after grid + barrier_extra arrivals and waits at
+// most 2^barrier_shift SM cycles: 0 and 32 in production; the test hook
+// bubble_ext_test_expire_batch_barrier passes 1 (no arrival releases it) and
+// a short limit.
 int batch_max_grid(bool fast, int ty);
 size_t batch_smem_bytes(int ty);
 cudaError_t batch_launch(bool fast, int ty, const void *lat, int n_lat, int n_items, int steps,
-                         unsigned int *counters, int *status, int grid, cudaStream_t s);
+                         unsigned int *counters, int *status, int grid, unsigned int barrier_extra,
+                         int barrier_shift, cudaStream_t s);
 
 }  // namespace launch
 }  // namespace bubble
@@ -102,6 +92,7 @@ namespace launch {
 // strict-mode halves of the batch entry points (kernels_strict.cu)
 int batch_max_grid_strict(int ty);
 cudaError_t batch_launch_strict(int ty, const void *lat, int n_lat, int n_items, int steps,
-                                unsigned int *counters, int *status, int grid, cudaStream_t s);
+                                unsigned int *counters, int *status, int grid, unsigned int barrier_extra,
+                                int barrier_shift, cudaStream_t s);
 }  // namespace launch
 }  // namespace bubble

@@ -85,21 +85,6 @@ cudaError_t stage_ref(const StageArgs<R> &A, const V4<R> *prim, const LatticePar
 }
 
 template <typename R, bool FAST, int MIXED, int TY>
-cudaError_t stage_fused(const StageArgs<R> &A, const LatticeParams<R> &P, int lz, cudaStream_t s) {
-    constexpr int TX = 32;
-    using L = dev::FusedLayout<R, TX, TY>;
-    auto k = dev::stage_fused_kernel<R, FAST, MIXED, TX, TY>;
-    cudaError_t e = ensure_smem(k, L::bytes);
-    if (e != cudaSuccess) return e;
-    if (lz < 1) lz = 1;
-    const int ntx = (P.nx + TX - 1) / TX, nty = (P.ny + TY - 1) / TY;
-    const int nzc = (P.nz + lz - 1) / lz;
-    dim3 grid(ntx * nty, nzc);
-    k<<<grid, L::NT, L::bytes, s>>>(A, P, lz);
-    return cudaGetLastError();
-}
-
-template <typename R, bool FAST, int MIXED, int TY>
 cudaError_t stage_v2(const StageArgs<R> &A, const LatticeParams<R> &P, int lz, const StageMaps &maps, int tma_ok,
                      int *status, cudaStream_t s) {
     using L = dev::V2Layout<R, TY>;
@@ -146,14 +131,14 @@ int batch_max_grid() {
 
 template <bool FAST, int TY>
 cudaError_t batch_launch(const void *lat, int n_lat, int n_items, int steps, unsigned int *counters,
-                         int *status, int grid, cudaStream_t s) {
+                         int *status, int grid, unsigned int barrier_extra, int barrier_shift, cudaStream_t s) {
     using L = dev::V2Layout<float, TY>;
     auto k = dev::batch_v2_kernel<FAST, TY>;
     cudaError_t e = ensure_smem(k, L::bytes);
     if (e != cudaSuccess) return e;
     const BatchLattice *lp = static_cast<const BatchLattice *>(lat);
-    void *args[] = {(void *)&lp, (void *)&n_lat, (void *)&n_items, (void *)&steps, (void *)&counters,
-                    (void *)&status};
+    void *args[] = {(void *)&lp,       (void *)&n_lat,  (void *)&n_items,       (void *)&steps,
+                    (void *)&counters, (void *)&status, (void *)&barrier_extra, (void *)&barrier_shift};
     return cudaLaunchCooperativeKernel((const void *)k, dim3(grid), dim3(L::NT), args, L::bytes, s);
 }
 

@@ -58,6 +58,12 @@ struct StageArgs {
     V4<R> *fluid_out;
     R a0, a1, dt;
     int32_t stage;  // 0, 1, 2; stage 0 has a0 == 0 and never reads U^n
+    // Bounded waits of the stage kernel give up after 2^wait_shift SM cycles.
+    // Test hook (bubble_ext_test_expire_stage_wait): when test_tx != 0, every
+    // CTA staging planes through TMA arms its first plane's mbarrier for
+    // test_tx bytes and issues no copy for it, so that wait expires.
+    uint32_t test_tx = 0;
+    int32_t wait_shift = 31;
 };
 
 // Result of the diagnostics reduction (shaders/reduce.wgsl:32-38), with FP64

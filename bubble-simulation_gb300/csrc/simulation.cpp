@@ -207,8 +207,8 @@ int Simulation::allocate(std::string &err) {
     return BUBBLE_OK;
 }
 
-LatticeParams<float> Simulation::params_f32() const {
-    const SimParamsHost h = sim_params(spec_.model, grid_);
+LatticeParams<float> lattice_params_f32(const bubble_spec &spec) {
+    const SimParamsHost h = sim_params(spec.model, spec.grid);
     LatticeParams<float> p{};
     p.nx = (int)h.nx;
     p.ny = (int)h.ny;
@@ -225,12 +225,12 @@ LatticeParams<float> Simulation::params_f32() const {
     p.e_floor = h.e_floor;
     p.z_max = h.z_max;
     p.e_ref = h.e_ref;
-    if (spec_.eos == BUBBLE_EOS_GAMMA_LAW) {
-        p.eos_c2 = spec_.eos_param[0] - 1.0f;
-        p.eos_e0 = spec_.eos_param[1];
+    if (spec.eos == BUBBLE_EOS_GAMMA_LAW) {
+        p.eos_c2 = spec.eos_param[0] - 1.0f;
+        p.eos_e0 = spec.eos_param[1];
     }
-    if (spec_.eos == BUBBLE_EOS_THERMAL) {
-        const float g = spec_.eos_param[0], a = spec_.eos_param[1];
+    if (spec.eos == BUBBLE_EOS_THERMAL) {
+        const float g = spec.eos_param[0], a = spec.eos_param[1];
         p.th_k = h.a_rad / 3.0f;
         p.th_g = g;
         p.th_h = a / 3.0f;
@@ -240,7 +240,7 @@ LatticeParams<float> Simulation::params_f32() const {
         p.a_rad = h.a_rad;
         p.t_ref = h.t_ref;
     }
-    if (spec_.precision == BUBBLE_PRECISION_PERTURBATION) {
+    if (spec.precision == BUBBLE_PRECISION_PERTURBATION) {
         // the stored energy is E - e_bg and the primitive pressure p - p_bg;
         // the floors move with them
         p.e_bg = h.e_ref;
@@ -251,18 +251,18 @@ LatticeParams<float> Simulation::params_f32() const {
     return p;
 }
 
-int Simulation::arith_mode() const {
-    if (spec_.eos == BUBBLE_EOS_GAMMA_LAW) return 3;
-    if (spec_.eos == BUBBLE_EOS_THERMAL) return 4;
-    switch (spec_.precision) {
+int arith_mode(const bubble_spec &spec) {
+    if (spec.eos == BUBBLE_EOS_GAMMA_LAW) return 3;
+    if (spec.eos == BUBBLE_EOS_THERMAL) return 4;
+    switch (spec.precision) {
         case BUBBLE_PRECISION_MIXED: return 1;
         case BUBBLE_PRECISION_PERTURBATION: return 2;
         default: return 0;
     }
 }
 
-LatticeParams<double> Simulation::params_f64() const {
-    const LatticeParams<float> f = params_f32();
+LatticeParams<double> lattice_params_f64(const bubble_spec &spec) {
+    const LatticeParams<float> f = lattice_params_f32(spec);
     LatticeParams<double> p{};
     p.nx = f.nx;
     p.ny = f.ny;
@@ -281,6 +281,10 @@ LatticeParams<double> Simulation::params_f64() const {
     p.e_ref = f.e_ref;
     return p;
 }
+
+LatticeParams<float> Simulation::params_f32() const { return lattice_params_f32(spec_); }
+LatticeParams<double> Simulation::params_f64() const { return lattice_params_f64(spec_); }
+int Simulation::arith_mode() const { return bubble::arith_mode(spec_); }
 
 int Simulation::launch_init(std::string &err) {
     cudaError_t e;
@@ -421,11 +425,10 @@ int Simulation::record_nucleation(std::string &err) {
 int Simulation::stage_launch(int stage, uint32_t in_slot, uint32_t out_slot, std::string &err) {
     const uint64_t n = n_cells_;
     cudaError_t e = cudaSuccess;
-    const bool mixed = spec_.precision == BUBBLE_PRECISION_MIXED;
     const int mode = arith_mode();
-    if (mode >= 2 && path_ != KernelPath::Fused) {
-        err = "the perturbation form and the gamma-law and thermal equations of state run on the default "
-              "(fused, asynchronous staging) kernel path only";
+    if (mode != 0 && path_ != KernelPath::Fused) {
+        err = "the MIXED and perturbation forms and the gamma-law and thermal equations of state run on the "
+              "default (fused) kernel path only";
         return BUBBLE_ERR_INVALID;
     }
     if (is_f64()) {
@@ -441,14 +444,13 @@ int Simulation::stage_launch(int stage, uint32_t in_slot, uint32_t out_slot, std
         A.a1 = rk[stage][1];
         A.dt = (double)derive(spec_.model).dt;
         A.stage = stage;
+        A.test_tx = test_tx_;
+        A.wait_shift = test_tx_ ? test_shift_ : 31;
         const LatticeParams<double> P = params_f64();
         if (path_ == KernelPath::Reference) {
             e = launch::prim_f64(A.fluid_in, (V4<double> *)prim_, n, P, stream_);
             if (e == cudaSuccess) e = launch::stage_ref_f64(A, (const V4<double> *)prim_, P, stream_);
             launches_ += 2;
-        } else if (path_ == KernelPath::FusedSync) {
-            e = launch::stage_fused_f64(A, P, tile_, stream_);
-            launches_ += 1;
         } else {
             e = launch::stage_v2_f64(A, P, tile_, maps_[in_slot], tma_ok_ ? 1 : 0, d_status_, stream_);
             launches_ += 1;
@@ -465,15 +467,13 @@ int Simulation::stage_launch(int stage, uint32_t in_slot, uint32_t out_slot, std
         A.a1 = kRK3[stage][1];
         A.dt = derive(spec_.model).dt;
         A.stage = stage;
+        A.test_tx = test_tx_;
+        A.wait_shift = test_tx_ ? test_shift_ : 31;
         const LatticeParams<float> P = params_f32();
         if (path_ == KernelPath::Reference) {
             e = launch::prim_f32(A.fluid_in, (V4<float> *)prim_, n, P, stream_);
             if (e == cudaSuccess) e = launch::stage_ref_f32(A, (const V4<float> *)prim_, P, stream_);
             launches_ += 2;
-        } else if (path_ == KernelPath::FusedSync) {
-            if (spec_.math == BUBBLE_MATH_STRICT) e = launch::stage_fused_f32_strict(A, P, tile_, mixed, stream_);
-            else e = launch::stage_fused_f32_fast(A, P, tile_, mixed, stream_);
-            launches_ += 1;
         } else {
             const int tma = tma_ok_ ? 1 : 0;
             if (spec_.math == BUBBLE_MATH_STRICT)
@@ -483,6 +483,7 @@ int Simulation::stage_launch(int stage, uint32_t in_slot, uint32_t out_slot, std
             launches_ += 1;
         }
     }
+    test_tx_ = 0;  // the test hook arms one launch
     BUBBLE_CUDA(e, "stage kernel");
     return BUBBLE_OK;
 }

@@ -28,7 +28,6 @@ namespace bubble {
 enum class KernelPath : int {
     Fused = 0,      // one fused launch per RK stage with async staging (default)
     Reference = 1,  // primitives pass + stage pass per RK stage, as in the reference
-    FusedSync = 2,  // the fused kernel with synchronous plane staging
 };
 
 class Simulation {
@@ -53,6 +52,14 @@ class Simulation {
     void device_state(void **field, void **fluid) const;
 
     void set_path(KernelPath p) { path_ = p; }
+    // Test hook: the next stage launch arms, in every CTA that stages planes
+    // through TMA, its first plane's mbarrier for `tx` bytes with no copy
+    // issued, and bounds the stage kernel's waits by 2^shift SM cycles, so
+    // those waits expire and the next check reports BUBBLE_ERR_TIMEOUT.
+    void arm_wait_expiry(uint32_t tx, int shift) {
+        test_tx_ = tx;
+        test_shift_ = shift;
+    }
     KernelPath path() const { return path_; }
     int set_tile(TileShape t, std::string &err);
     TileShape tile() const { return tile_; }
@@ -116,6 +123,8 @@ class Simulation {
     size_t next_event_ = 0;
     bool nucleated_this_frame_ = false;
     KernelPath path_ = KernelPath::Fused;
+    uint32_t test_tx_ = 0;  // 0: the wait-expiry test hook is off
+    int test_shift_ = 31;
     TileShape tile_{32, 8, 64};
 
     // device memory
@@ -147,6 +156,13 @@ class Simulation {
     bool own_stream_ = false;
     uint64_t launches_ = 0;
 };
+
+// Kernel constants of a lattice described by `spec` (its grid, model,
+// precision form and equation of state), and the FORM parameter of the
+// kernels (physics.cuh kPlain, kMixed, kPert, kGamma, kThermal).
+LatticeParams<float> lattice_params_f32(const bubble_spec &spec);
+LatticeParams<double> lattice_params_f64(const bubble_spec &spec);
+int arith_mode(const bubble_spec &spec);
 
 // Default z chunk of the fused kernel for a lattice: enough CTAs to fill the
 // GPU several times over while keeping the 4-plane warm-up of each chunk a

@@ -63,11 +63,13 @@ BUBBLE_DEV bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait: ~2^31 SM cycles (about a second at GB300 clocks).
-BUBBLE_DEV bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+// Bounded wait: gives up after 2^shift SM cycles (2^31 by default, about a
+// second at GB300 clocks).
+BUBBLE_DEV bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int shift) {
     const long long start = clock64();
+    const long long limit = 1ll << shift;
     while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - start > (1ll << 31)) return false;
+        if (clock64() - start > limit) return false;
     }
     return true;
 }
@@ -272,9 +274,14 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
         if (tma) {
             if (t == 0) {
                 fence_proxy_async();
-                mbar_expect_tx(&bar[s], L::plane_tx_bytes);
-                tma_load_4d(raw_u + s * PC, &maps->fluid, &bar[s], 0, x0 - 2, y0 - 2, gz);
-                tma_load_3d(raw_f + s * PC, &maps->field, &bar[s], 2 * (x0 - 2), y0 - 2, gz);
+                if (A.test_tx != 0 && p == z0 + 3) {
+                    // test hook: bytes that no copy delivers, and no copy issued
+                    mbar_expect_tx(&bar[s], A.test_tx);
+                } else {
+                    mbar_expect_tx(&bar[s], L::plane_tx_bytes);
+                    tma_load_4d(raw_u + s * PC, &maps->fluid, &bar[s], 0, x0 - 2, y0 - 2, gz);
+                    tma_load_3d(raw_f + s * PC, &maps->field, &bar[s], 2 * (x0 - 2), y0 - 2, gz);
+                }
             }
         } else {
             const size_t base = (size_t)gz * plane;
@@ -293,7 +300,7 @@ BUBBLE_DEV bool v2_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
     auto wait_plane = [&](int p) -> bool {
         if (tma) {
             const uint32_t parity = ((p - (z0 + 3)) >> 1) & 1;
-            return mbar_wait_bounded(&bar[raw_slot(p)], parity);
+            return mbar_wait_bounded(&bar[raw_slot(p)], parity, A.wait_shift);
         }
         cp_async_wait_all();
         return true;

@@ -52,6 +52,14 @@ int bubble_batch_load_state(bubble_batch *batch, uint32_t index, const float *fi
 int bubble_batch_info_get(const bubble_batch *batch, bubble_batch_info *out);
 float bubble_batch_time(const bubble_batch *batch, uint32_t index);
 
+/* Test hook of the persistent launch's bounded grid barrier: the next
+ * launch of `batch` runs its barrier with a release count one above the
+ * grid, so no arrival releases it, and a wait limit of 2^wait_shift SM
+ * cycles (10..32); every CTA's wait expires, sets the status word and
+ * returns, and the next bubble_batch_diagnostics reports BUBBLE_ERR_TIMEOUT.  Lattices that run solo (fill the GPU alone) do not use
+ * the persistent launch. */
+int bubble_ext_test_expire_batch_barrier(bubble_batch *batch, int32_t wait_shift);
+
 /* Fastest z chunk of the fused stage kernel for a lattice size (autotuner,
  * cached per process). */
 int bubble_autotune_chunk(const uint32_t grid[3], int32_t tile_y, int32_t math, int32_t *lz_out);

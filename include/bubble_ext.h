@@ -18,9 +18,8 @@ extern "C" {
 /* Kernel path of the RK stages. */
 #define BUBBLE_PATH_FUSED 0     /* one fused launch per stage (default)       */
 #define BUBBLE_PATH_REFERENCE 1 /* primitives pass + stage pass per stage,
-                                   the reference's own kernel structure      */
-#define BUBBLE_PATH_FUSED_SYNC 2 /* the fused kernel staging planes with
-                                    synchronous loads (for comparison)       */
+                                   the reference's own kernel structure (bag
+                                   model, SINGLE and DOUBLE only)            */
 int bubble_ext_set_path(bubble_sim *sim, int32_t path);
 
 /* Tile of the fused kernel: y extent (4 or 8 for FP32, 4 for FP64; x is 32)
@@ -38,6 +37,19 @@ uint64_t bubble_ext_launches(const bubble_sim *sim);
 /* Make the next device allocation of this process fail (host-side fault
  * injection for the failure-handling tests). */
 void bubble_ext_inject_allocation_failure(void);
+
+/* Test hook of the stage kernel's bounded waits (the device side of the
+ * reference's failure path, src/headless.rs:63-67, which stops a run whose
+ * diagnostics go bad).  The next stage launch of `sim` arms, in every CTA
+ * that stages planes through TMA, its first plane's mbarrier for
+ * `extra_bytes` (1..65536) bytes that no copy will deliver -- no copy is
+ * issued for that plane -- and limits the kernel's waits to 2^wait_shift SM
+ * cycles (10..31).  Those waits expire, the CTAs set the status word and
+ * return with nothing in flight, and the next bubble_synchronize or
+ * bubble_diagnostics returns BUBBLE_ERR_TIMEOUT; the context stays usable.
+ * Lattices whose tiles all touch the periodic boundary (x < 68 cells or
+ * y < 12) have no TMA tile, and the hook then changes nothing. */
+int bubble_ext_test_expire_stage_wait(bubble_sim *sim, uint32_t extra_bytes, int32_t wait_shift);
 
 /* Raw FP64 result of the diagnostics reduction: sums over cells of the
  * total energy density, broken-phase indicator, fluid kinetic energy
@@ -58,20 +70,23 @@ typedef struct bubble_diag_raw {
  * For engines that own all device memory through their own pool, real-time
  * loops that must not allocate mid-run, or hosts with a fixed memory
  * budget: the caller passes its own device buffers -- `field` (2 values per
- * cell) and `fluid` (4 per cell), float for BUBBLE_PRECISION_SINGLE/MIXED,
- * double for BUBBLE_PRECISION_DOUBLE, in the lattice order of this header --
- * and a device pointer `result` to one bubble_diag_raw; the launch goes on
- * `stream` (a cudaStream_t, NULL for the default stream) and is
- * asynchronous.  The call allocates nothing: its scratch (1024 block
+ * cell) and `fluid` (4 per cell), float for the FP32 forms, double for
+ * BUBBLE_PRECISION_DOUBLE, in the lattice order of this header -- the
+ * lattice's `spec` (grid, model, precision form and equation of state, as
+ * given to bubble_create; the schedule fields are not read) and a device
+ * pointer `result` to one bubble_diag_raw.  The sums are those
+ * bubble_diagnostics reports for the same state and spec (for the
+ * perturbation form they include the background energy N e_ref).  The
+ * launch goes on `stream` (a cudaStream_t, NULL for the default stream) and
+ * is asynchronous.  The call allocates nothing: its scratch (1024 block
  * partials and a completion counter, 49,408 bytes) is a static device array
  * of the library, held on every GPU that loads the library until exit.
- * Any lattice with axes 8..2048 fits; other sizes are rejected with
- * BUBBLE_ERR_INVALID.  The first call on a device looks up the scratch
- * address and loads the module there: make it before any stream capture.
- * All calls share the scratch: the counter is cleared on `stream` before
- * each launch, and calls that overlap on the GPU race. */
-int bubble_diagnostics_noalloc(const void *field, const void *fluid, const uint32_t grid[3],
-                               const bubble_model *model, int32_t precision, void *result,
+ * Any lattice with axes 8..2048 fits; other sizes, and specs that
+ * bubble_create would refuse, are rejected with BUBBLE_ERR_INVALID.  The
+ * first call on a device loads the module there: make it before any stream
+ * capture.  All calls share the scratch: the counter is cleared on `stream`
+ * before each launch, and calls that overlap on the GPU race. */
+int bubble_diagnostics_noalloc(const void *field, const void *fluid, const bubble_spec *spec, void *result,
                                void *stream);
 
 #ifdef __cplusplus

@@ -17,6 +17,8 @@
 //   nucleate main, min_image     shaders/nucleate.wgsl:51-85
 //   cell_contribution, reduce    shaders/reduce.wgsl:49-140 (sums in FP64)
 //   vis main                     shaders/vis.wgsl:30-55 (binary16 round to nearest even)
+//   MIXED form's FP64 recovery   shaders/eos.wgsl:94-123 in FP64 where the
+//                                FP32 v^2 > 8/9 (docs/PRECISION.md:150-152)
 //   fs_main and helpers          shaders/volume.wgsl:80-381, with the
 //                                sampler of src/gpu/render.rs:206-218
 //                                (trilinear, clamp to edge) in software
@@ -601,12 +603,56 @@ void step_all(const SimParams<R> &P, const StageParams<R> &S, const R *field_n, 
                                                    fluid_out, x, y, z);
 }
 
-template <typename R, bool PERT = false, bool GAMMA = false, bool THERMAL = false>
+// ---------------------------------------------------------------------------
+//  MIXED precision form: FP64 recovery where the Lorentz factor exceeds 3
+// ---------------------------------------------------------------------------
+// The FP32 recovery is redone in FP64 from the same FP32 conserved state
+// wherever the FP32 result has v^2 > 8/9 (gamma > 3), where E^2 - Z^2
+// cancels and FP32 loses the pressure; the reference's precision plan puts
+// FP64 at exactly this inversion (docs/PRECISION.md:150-152).  The FP64 steps
+// are eos_regularise and eos_pressure_from_conserved (shaders/eos.wgsl:
+// 94-123) on the FP32 inputs and constants widened exactly, the result rounded
+// once to FP32.  PERT: the perturbation form's inversion (as
+// eos_prim_from_cons_pert) with p_bg the FP32 value of e_ref / 3 widened.
+template <bool PERT>
+inline vec4<float> prim_from_cons_f64(const SimParams<float> &P, vec4<float> u) {
+    const double e_bg = PERT ? (double)P.e_ref : 0.0;
+    const double p_bg = PERT ? (double)(P.e_ref / 3.0f) : 0.0;
+    const double de = wmax((double)u.x, (double)P.e_floor);
+    const double e_lab = PERT ? e_bg + de : de;
+    double zx = u.y, zy = u.z, zz = u.w;
+    const double zlen = length3(zx, zy, zz);
+    const double zcap = (double)P.z_max * e_lab;
+    if (zlen > zcap) {
+        const double s = zcap / wmax(zlen, 1e-30);
+        zx = zx * s;
+        zy = zy * s;
+        zz = zz * s;
+    }
+    const double z2 = zx * zx + zy * zy + zz * zz;
+    double p;
+    if (PERT) {
+        const double sq = std::sqrt(wmax(4.0 * e_lab * e_lab - 3.0 * z2, 0.0));
+        p = de / 3.0 - z2 / (sq + 2.0 * e_lab);
+    } else {
+        const double disc = wmax(4.0 * e_lab * e_lab - 3.0 * z2, 0.0);
+        p = (e_lab * e_lab - z2) / (e_lab + std::sqrt(disc));
+    }
+    p = wmax(p, (double)P.p_floor);
+    const double d = PERT ? wmax(e_lab + p_bg + p, 1e-30) : wmax(e_lab + p, 1e-30);
+    return {(float)(zx / d), (float)(zy / d), (float)(zz / d), (float)p};
+}
+
+template <typename R, bool PERT = false, bool GAMMA = false, bool THERMAL = false, bool MIXED = false>
 void primitives_all(const SimParams<R> &P, const R *field, const R *fluid, R *prim) {
     const size_t n = (size_t)P.nx * P.ny * P.nz;
 #pragma omp parallel for schedule(static)
     for (long long i = 0; i < (long long)n; ++i) {
-        const vec4<R> q = eos_prim_from_cons<R, PERT, GAMMA, THERMAL>(P, ld4(fluid, (size_t)i), field[2 * i]);
+        vec4<R> q = eos_prim_from_cons<R, PERT, GAMMA, THERMAL>(P, ld4(fluid, (size_t)i), field[2 * i]);
+        if constexpr (MIXED && sizeof(R) == 4) {
+            const R v2 = q.x * q.x + q.y * q.y + q.z * q.z;
+            if (v2 > R(8.0) / R(9.0)) q = prim_from_cons_f64<PERT>(P, ld4(fluid, (size_t)i));
+        }
         prim[4 * i] = q.x;
         prim[4 * i + 1] = q.y;
         prim[4 * i + 2] = q.z;
@@ -1069,8 +1115,10 @@ void oracle_init_pert_f32(const SimParams<float> *P, float *field, float *fluid)
     const size_t n = (size_t)P->nx * P->ny * P->nz;
     for (size_t i = 0; i < n; ++i) fluid[4 * i] = 0.0f;
 }
+// The perturbation form is the MIXED form over E - e_ref: FP64 recovery
+// where v^2 > 8/9.
 void oracle_primitives_pert_f32(const SimParams<float> *P, const float *field, const float *fluid, float *prim) {
-    primitives_all<float, true>(pert_params(*P), field, fluid, prim);
+    primitives_all<float, true, false, false, true>(pert_params(*P), field, fluid, prim);
 }
 void oracle_step_pert_f32(const SimParams<float> *P, const StageParams<float> *S, const float *field_n,
                           const float *fluid_n, const float *field_in, const float *fluid_in, const float *prim,
@@ -1084,6 +1132,12 @@ void oracle_reduce_pert_f32(const SimParams<float> *P, const float *field, const
 void oracle_vis_pert_f32(const SimParams<float> *P, const float *field, const float *fluid, const float *prim,
                          uint16_t *out) {
     vis_all<float, true>(pert_params(*P), field, fluid, prim, out);
+}
+
+// The MIXED precision form: the FP32 kernels with the primitives pass
+// recovering in FP64 where v^2 > 8/9 (step, reduce and vis read its output).
+void oracle_primitives_mixed_f32(const SimParams<float> *P, const float *field, const float *fluid, float *prim) {
+    primitives_all<float, false, false, false, true>(*P, field, fluid, prim);
 }
 
 void oracle_vis_f32(const SimParams<float> *P, const float *field, const float *fluid, const float *prim,

@@ -78,6 +78,7 @@ def lib() -> ctypes.CDLL:
         L.oracle_set_threads.argtypes = [ctypes.c_int]
         L.oracle_set_eos.argtypes = [ctypes.c_float] * 3
         L.oracle_primitives_gamma_f32.argtypes = [P, P, P, P]
+        L.oracle_primitives_mixed_f32.argtypes = [P, P, P, P]
         L.oracle_step_gamma_f32.argtypes = [P] * 9
         L.oracle_set_thermal.argtypes = [ctypes.c_float] * 6
         L.oracle_init_thermal_f32.argtypes = [P, P, P]
@@ -340,9 +341,10 @@ class OracleSim:
 
     def __init__(self, grid, model: dict | None = None, schedule=None, precision: str = "f32",
                  eos: tuple = ("bag", 1.0, 0.0)):
-        """precision: "f32", "f64", or "pert" (FP32 perturbation form: the
-        fluid energy stored as E - e_ref, include/bubble.h
-        BUBBLE_PRECISION_PERTURBATION without its FP64 fallback).
+        """precision: "f32", "f64", "mixed" (FP32 with the primitive recovery
+        redone in FP64 where v^2 > 8/9, include/bubble.h
+        BUBBLE_PRECISION_MIXED) or "pert" (the MIXED form with the fluid
+        energy stored as E - e_ref, BUBBLE_PRECISION_PERTURBATION).
         eos: ("bag", -, -), ("bag_dof", ratio, -), ("gamma_law", Gamma, e0) or
         ("thermal", gamma, A) (include/bubble.h BUBBLE_EOS_*; the gamma law and
         the thermal potential in FP32 only)."""
@@ -355,13 +357,20 @@ class OracleSim:
             raise ValueError(err)
         self.grid = tuple(int(g) for g in grid)
         self.n = self.grid[0] * self.grid[1] * self.grid[2]
+        if precision not in ("f32", "f64", "mixed", "pert"):
+            raise ValueError(f"unknown precision {precision!r}")
         self.pert = precision == "pert"
+        self.mixed = precision == "mixed"
         self.dtype = np.float64 if precision == "f64" else np.float32
         self.sfx = "f64" if precision == "f64" else "f32"
         self.ksfx = "pert_f32" if self.pert else self.sfx  # kernels that differ in the perturbation form
         self.gsfx = "gamma_f32" if self.gamma else self.ksfx  # kernels that differ for the gamma law
         if self.thermal:  # every kernel but init and nucleation differs for the thermal potential
             self.gsfx = self.ksfx = "thermal_f32"
+        # the primitives pass is the one kernel of the MIXED form that differs
+        self.psfx = "mixed_f32" if self.mixed else self.gsfx
+        if self.mixed and (self.gamma or self.thermal):
+            raise ValueError("the MIXED form is the bag model's")
         self.d = derived(self.model)
         self.P = _sim_params(self.dtype, self.model, self.grid)
         self.field = np.zeros((3, self.n, 2), dtype=self.dtype)
@@ -407,7 +416,7 @@ class OracleSim:
         self._set_eos()
         a0, a1 = (RK3_F32 if self.dtype == np.float32 else RK3_F64)[stage]
         S = np.array([a0, a1, self.d["dt"], 0.0], dtype=self.dtype)
-        getattr(L, f"oracle_primitives_{self.gsfx}")(_ptr(self.P), _ptr(self.field[in_slot]),
+        getattr(L, f"oracle_primitives_{self.psfx}")(_ptr(self.P), _ptr(self.field[in_slot]),
                                                     _ptr(self.fluid[in_slot]), _ptr(self.prim))
         getattr(L, f"oracle_step_{self.gsfx}")(
             _ptr(self.P), _ptr(S), _ptr(self.field[self.cur]), _ptr(self.fluid[self.cur]),
@@ -451,7 +460,7 @@ class OracleSim:
         (binary16 bits of phi/phi_b, |v|, T/T_ref - 1, (E+p)v^2/e_ref)."""
         L = lib()
         self._set_eos()
-        getattr(L, f"oracle_primitives_{self.gsfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
+        getattr(L, f"oracle_primitives_{self.psfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
                                                     _ptr(self.fluid[self.cur]), _ptr(self.prim))
         nx, ny, nz = self.grid
         out = np.zeros((nz, ny, nx, 4), dtype=np.uint16)
@@ -463,7 +472,7 @@ class OracleSim:
     def diagnostics(self) -> dict:
         L = lib()
         self._set_eos()
-        getattr(L, f"oracle_primitives_{self.gsfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
+        getattr(L, f"oracle_primitives_{self.psfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
                                                     _ptr(self.fluid[self.cur]), _ptr(self.prim))
         sums = np.zeros(4, dtype=np.float64)
         vmax = np.zeros(1, dtype=self.dtype)

@@ -1,6 +1,6 @@
 """Generate the committed golden fixtures from the oracle and the reference's docs.
 
-    python tests/golden/make_golden.py [--reference DIR] [--skip-128]
+    python tests/golden/make_golden.py --reference DIR [--skip-128]
 
 Writes into tests/golden/:
   published_numerics.json  the reference's published single-bubble and
@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import os
 import re
 import sys
 import time
@@ -82,6 +83,47 @@ def perturbed_state(sim: "oracle.OracleSim", seed: int, amp: float) -> None:
     sim.fluid[sim.cur] = fluid.reshape(-1, 4).astype(sim.dtype)
 
 
+def relativistic_state(sim: "oracle.OracleSim", seed: int, v_peak: float = 0.995) -> int:
+    """Add a smooth relativistic blob to the current slot: inside a seeded ball
+    of radius R (a third of the shortest axis) the fluid moves along a seeded
+    direction at |v| = v_peak up to R/2 and v_peak cos^2 beyond, reaching 0
+    at R, at 1 to 1.5 times the background pressure, so the ball holds cells
+    at every Lorentz factor from 1 to 1/sqrt(1 - v_peak^2) (gamma > 3 where
+    |v| > 0.943).  Conserved variables
+    are built in FP64 from (v, p) (bag model: w = 4p, E = w W^2 - p,
+    Z = w W^2 v) and rounded once.  Returns the number of cells whose FP32
+    recovery gives v^2 > 8/9."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = sim.grid
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    c = rng.uniform(0.3, 0.7, size=3) * np.array([nx, ny, nz])
+    rad = max(min(nx, ny, nz) / 3.0, 4.0)
+    d = [np.minimum(np.abs(a - ca), n - np.abs(a - ca)) for a, ca, n in ((x, c[0], nx), (y, c[1], ny), (z, c[2], nz))]
+    r = np.sqrt(d[0] ** 2 + d[1] ** 2 + d[2] ** 2)
+    inside = r < rad
+    ramp = np.cos(np.pi * np.clip(r / rad - 0.5, 0.0, 0.5)) ** 2
+    speed = np.where(inside, v_peak * ramp, 0.0)
+    n = rng.normal(size=3)
+    n /= np.linalg.norm(n)
+    e_ref = float(sim.d["e_ref"])
+    p = e_ref / 3.0 * (1.0 + 0.5 * np.where(inside, ramp, 0.0))
+    w2 = 1.0 / (1.0 - speed ** 2)
+    ww = 4.0 * p * w2
+    fluid = sim.fluid[sim.cur].reshape(nz, ny, nx, 4).astype(np.float64)
+    sel = inside
+    fluid[..., 0] = np.where(sel, ww - p - (e_ref if sim.pert else 0.0), fluid[..., 0])
+    for k in range(3):
+        fluid[..., 1 + k] = np.where(sel, ww * speed * n[k], fluid[..., 1 + k])
+    sim.fluid[sim.cur] = fluid.reshape(-1, 4).astype(sim.dtype)
+    # cells the FP32 recovery puts above gamma = 3
+    u = sim.fluid[sim.cur].astype(np.float64)
+    e = np.maximum(u[:, 0] + (e_ref if sim.pert else 0.0), 1e-30)
+    z2 = (u[:, 1:] ** 2).sum(axis=1)
+    pp = (e * e - z2) / (e + np.sqrt(np.maximum(4 * e * e - 3 * z2, 0)))
+    v2 = z2 / (e + pp) ** 2
+    return int((v2 > 8.0 / 9.0).sum())
+
+
 CASES = [
     # name, grid, bubbles (centre mode, radius), steps, velocity amplitude, seed
     ("odd", (9, 11, 13), 3.5, 12, 0.30, 1),
@@ -112,9 +154,12 @@ def make_cases() -> dict:
 
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("BUBBLE_REFERENCE"),
+                    help="the reference source tree (default: $BUBBLE_REFERENCE)")
     ap.add_argument("--skip-128", action="store_true")
     a = ap.parse_args()
+    if not a.reference:
+        ap.error("--reference (or BUBBLE_REFERENCE) must name the reference source tree")
     oracle.build()
     pub = parse_tables(Path(a.reference) / "docs" / "NUMERICS.md")
     pub["threshold_700"] = parse_threshold(Path(a.reference) / "docs" / "PHYSICS.md")

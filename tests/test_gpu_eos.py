@@ -96,7 +96,7 @@ def test_gamma_law_rejects_other_paths(bubble, gpu):
     with sim(bubble, (16, 16, 16), "gamma_law", (1.5, 0.0), math="fast") as s:
         with pytest.raises(bubble.BubbleError):
             s.set_tile(4, 16)
-        s.set_path("fused_sync")
+        s.set_path("reference")
         with pytest.raises(bubble.BubbleError):
             s.advance(1)
 

@@ -265,8 +265,7 @@ def test_nonfinite_state_is_reported(bubble, gpu):
 
 
 # ---- tile shapes and the full-size properties ------------------------------
-@pytest.mark.parametrize("path", ["fused", "fused_sync"])
-def test_tile_shapes_agree(bubble, gpu, golden, path):
+def test_tile_shapes_agree(bubble, gpu, golden):
     """Every z chunking of one kernel instantiation gives identical bits; the
     fast mode's two tile heights are separate instantiations whose FMA contraction may differ, so they agree
     within the fast-path bar, 1e-5 relative (measured: 1.6e-6 after 5 steps
@@ -277,7 +276,6 @@ def test_tile_shapes_agree(bubble, gpu, golden, path):
 
     def run(math, tile):
         with bubble.Simulation(spec_for(bubble, grid, "single", math)) as sim:
-            sim.set_path(path)
             sim.set_tile(*tile)
             sim.load_state(f0, u0)
             sim.advance(5)

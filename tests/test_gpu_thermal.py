@@ -127,6 +127,6 @@ def test_thermal_rejects_other_paths(bubble, gpu):
     with sim(bubble, (16, 16, 16), (0.01, 0.01), math="fast") as s:
         with pytest.raises(bubble.BubbleError):
             s.set_tile(4, 16)
-        s.set_path("fused_sync")
+        s.set_path("reference")
         with pytest.raises(bubble.BubbleError):
             s.advance(1)
