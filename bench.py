@@ -18,8 +18,10 @@ diagnostics readback every 10 steps, and the final state is copied back to
 pinned host memory, all inside the timed region.
 
 `--impl reference` times the CPU restatement of the reference's algorithm
-(the oracle; the reference itself is Rust/WGSL and cannot run here) on all
-host cores, each step one SSP-RK3 step of a 512x512x32 periodic slab.
+(the oracle's native build; the reference itself is Rust/WGSL and cannot
+run here) on all host cores, each step one SSP-RK3 step of the z < 32 slab
+of the workload's lattice as nucleated at t = 0 -- the same sample the GPU
+arm's cpu_baseline leg times.
 
 With --gpus N > 1 (under torchrun) every rank advances its own replica of
 the workload (the lattices are independent; no data-path collective):
@@ -179,20 +181,76 @@ def make_spec(bubble, wl: dict):
                                  seed=wl["seed"], precision=wl["precision"], math="fast")
 
 
-def cpu_baseline(state, wl: dict, seconds_budget: float = 20.0) -> dict:
-    """Time the FP32 oracle (all host cores) on a 512x512x32 slab of the warmed-up state."""
+def workload_slab(wl: dict, zs: int = 32, warm_steps: int = 2):
+    """The CPU baseline's sample of a workload: the z < zs slab of its lattice
+    (periodic in z over the slab) as nucleated at t = 0 by the workload's own
+    schedule (every bubble, minimum-image distances in the full lattice, the
+    reference's tanh profile), then warm_steps SSP-RK3 steps of the oracle.
+    Returns the warmed OracleSim on the native timing build.  Built on the
+    host alone, so the GPU arm's cpu_baseline leg and the reference arm time
+    exactly the same sample."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
 
-    oracle.build()
-    field, fluid = state
+    oracle.build(native=True)
     nx, ny, nz = wl["grid"]
-    zs = min(32, nz)
-    f = field.reshape(nz, ny, nx, 2)[:zs].reshape(-1, 2)
-    u = fluid.reshape(nz, ny, nx, 4)[:zs].reshape(-1, 4)
+    zs = min(zs, nz)
     m = dict(oracle.DEFAULT_MODEL, eta=wl["eta"])
-    sim = oracle.OracleSim((nx, ny, zs), model=m)
+    d = oracle.derived(m)
+    sched = oracle.make_schedule(wl["nucleation"], wl["bubbles"], d["seed_radius"], wl["grid"], wl["duration"],
+                                 wl["seed"])
+    phi = np.zeros((zs, ny, nx), dtype=np.float32)
+    phi_b, l_w, dx = float(m["phi_b"]), float(d["wall_width"]), float(m["dx"])
+
+    def min_image(a, n):
+        return (a + 0.5 * n) % n - 0.5 * n
+
+    for t, pos, r0 in sched:
+        if t > 0.0:
+            continue
+        cut = r0 * dx + 9.5 * l_w  # tanh saturates beyond: the profile is 0
+        span = int(math.ceil(cut / dx)) + 1
+        xs = np.arange(int(pos[0]) - span, int(pos[0]) + span + 1) % nx
+        ys = np.arange(int(pos[1]) - span, int(pos[1]) + span + 1) % ny
+        zz = np.arange(zs)
+        dzs = min_image(zz - pos[2], nz)
+        keep = np.abs(dzs) * dx < cut
+        if not keep.any():
+            continue
+        ddx = min_image(xs - pos[0], nx)[None, None, :]
+        ddy = min_image(ys - pos[1], ny)[None, :, None]
+        ddz = dzs[keep][:, None, None]
+        r = np.sqrt(ddx * ddx + ddy * ddy + ddz * ddz) * dx
+        prof = (0.5 * phi_b * (1.0 - np.tanh((r - r0 * dx) / l_w))).astype(np.float32)
+        sub = np.ix_(zz[keep], ys, xs)
+        phi[sub] = np.maximum(phi[sub], prof)
+    sim = oracle.OracleSim((nx, ny, zs), model=m, native=True)
+    f, u = sim.state()
+    f[:, 0] = phi.reshape(-1)
     sim.set_state(f, u)
+    for _ in range(warm_steps):
+        sim.record_step()
+    return sim
+
+
+def slab_sample_text(wl: dict, sim, threads: int) -> str:
+    import platform
+
+    nx, ny, zs = sim.grid
+    flag = "-mcpu=native" if platform.machine() in ("aarch64", "arm64") else "-march=native"
+    return (f"SSP-RK3 steps of the z<{zs} slab ({nx}x{ny}x{zs}, periodic) of the {wl['grid'][0]}x"
+            f"{wl['grid'][1]}x{wl['grid'][2]} workload nucleated at t=0 by its own schedule "
+            f"({wl['bubbles']} bubbles), warmed 2 steps; FP32 oracle (the reference's kernel structure: "
+            f"primitives pass, two HLL fluxes per face) built g++ -O3 {flag} -fopenmp, {threads} threads")
+
+
+def cpu_baseline(wl: dict, seconds_budget: float = 20.0) -> dict:
+    """Time the oracle's native build on all host cores over the workload's
+    CPU sample (workload_slab), and one step of its first planes on one
+    thread."""
+    sim = workload_slab(wl)
+    nx, ny, zs = sim.grid
+    threads = sim.L.oracle_threads()
     t0 = time.perf_counter()
     steps = 0
     while True:
@@ -202,22 +260,23 @@ def cpu_baseline(state, wl: dict, seconds_budget: float = 20.0) -> dict:
             break
     dt = time.perf_counter() - t0
     cells = nx * ny * zs
-    threads = oracle.lib().oracle_threads()
-    # the same slab's first 8 planes on one thread
+    # one thread: one step of the slab's first 8 planes
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    f, u = sim.state()
     z1 = min(8, zs)
-    sim1 = oracle.OracleSim((nx, ny, z1), model=m)
-    sim1.set_state(field.reshape(nz, ny, nx, 2)[:z1].reshape(-1, 2), fluid.reshape(nz, ny, nx, 4)[:z1].reshape(-1, 4))
-    oracle.lib().oracle_set_threads(1)
+    sim1 = oracle.OracleSim((nx, ny, z1), model=sim.model, native=True)
+    sim1.set_state(f.reshape(zs, ny, nx, 2)[:z1].reshape(-1, 2), u.reshape(zs, ny, nx, 4)[:z1].reshape(-1, 4))
+    sim.L.oracle_set_threads(1)
     t1 = time.perf_counter()
     sim1.record_step()
     dt1 = time.perf_counter() - t1
-    oracle.lib().oracle_set_threads(threads)
+    sim.L.oracle_set_threads(threads)
     return {"value": cells * steps / dt, "unit": "cell-updates/s", "cores": threads,
             "kind": "port", "value_1_thread": nx * ny * z1 / dt1, "cpu_model": cpu_model(),
-            "nproc": os.cpu_count(),
-            "sample": f"{steps} SSP-RK3 step(s) of a {nx}x{ny}x{zs} periodic slab of the warmed-up "
-                      f"{nx}x{ny}x{nz} state, FP32 oracle (reference kernel structure), "
-                      f"{threads} threads; value_1_thread: one step of its first {z1} planes on one thread"}
+            "nproc": os.cpu_count(), "sample": slab_sample_text(wl, sim, threads) +
+            f"; {steps} step(s) timed; value_1_thread: one step of its first {z1} planes on one thread"}
 
 
 def max_over_ranks(ms: float, dist, device: str) -> float:
@@ -251,21 +310,15 @@ def cpu_model() -> str:
 
 
 def run_reference(args, wl: dict, world: int, rank: int) -> int:
+    """The reference arm: its algorithm on the host cores (the oracle's native
+    build; the reference itself is Rust/WGSL and cannot run here), on the same
+    CPU sample as the GPU arm's cpu_baseline leg (workload_slab)."""
     if rank != 0:
         return 0
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle
-
-    oracle.build()
-    nx, ny, _ = wl["grid"]
-    zs = 32
-    m = dict(oracle.DEFAULT_MODEL, eta=wl["eta"])
-    d = oracle.derived(m)
-    sched = oracle.make_schedule(wl["nucleation"], min(wl["bubbles"], 8), d["seed_radius"],
-                                 (nx, ny, zs), wl["duration"], wl["seed"])
-    sim = oracle.OracleSim((nx, ny, zs), model=m, schedule=sched)
-    sim.record_nucleation()
-    for _ in range(args.warmup):
+    sim = workload_slab(wl)
+    nx, ny, zs = sim.grid
+    threads = sim.L.oracle_threads()
+    for _ in range(max(args.warmup - 2, 0)):
         sim.record_step()
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -273,15 +326,14 @@ def run_reference(args, wl: dict, world: int, rank: int) -> int:
     dt = time.perf_counter() - t0
     cells = nx * ny * zs
     value = cells * args.steps / dt
-    sample = (f"one SSP-RK3 step of a {nx}x{ny}x{zs} periodic slab per step (FP32 oracle, the "
-              f"reference's kernel structure, {oracle.lib().oracle_threads()} threads)")
+    sample = slab_sample_text(wl, sim, threads) + "; one slab step per step"
     line = {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": wl["name"], "sample_grid": [nx, ny, zs]},
-            "cpu_baseline": {"value": value, "unit": "cell-updates/s",
-                             "cores": oracle.lib().oracle_threads(), "kind": "port", "sample": sample},
+            "config": {"workload": wl["name"], "grid": list(wl["grid"]), "sample_grid": [nx, ny, zs]},
+            "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                             "sample": sample, "cpu_model": cpu_model()},
             "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -636,7 +688,7 @@ def main() -> int:
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(sim.copy_state(), wl)
+        cpu = cpu_baseline(wl)
 
     if rank == 0:
         line = {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,

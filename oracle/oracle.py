@@ -40,28 +40,44 @@ f32 = np.float32
 # ---------------------------------------------------------------------------
 
 
-def build(force: bool = False) -> Path:
-    """Compile oracle.cpp (g++ -O3 -fopenmp -ffp-contract=off) into lib/."""
+NATIVE_LIB_PATH = LIB_DIR / "liboracle_bubble_native.so"
+
+
+def _native_flags() -> list[str]:
+    """Tuning flags for the host CPU (the timed CPU baseline's build)."""
+    import platform
+
+    return ["-mcpu=native"] if platform.machine() in ("aarch64", "arm64") else ["-march=native"]
+
+
+def build(force: bool = False, native: bool = False) -> Path:
+    """Compile oracle.cpp into lib/.  The parity build (the checker) is
+    g++ -O3 -fopenmp -ffp-contract=off, one IEEE rounding per operation; the
+    native build (only ever timed, as the CPU baseline) adds the host CPU's
+    tuning flags and lets the compiler contract multiply-adds."""
     LIB_DIR.mkdir(exist_ok=True)
     src = HERE / "oracle.cpp"
-    if not force and LIB_PATH.exists() and LIB_PATH.stat().st_mtime >= src.stat().st_mtime:
-        return LIB_PATH
+    out = NATIVE_LIB_PATH if native else LIB_PATH
+    if not force and out.exists() and out.stat().st_mtime >= src.stat().st_mtime:
+        return out
     cxx = os.environ.get("CXX", "g++")
-    cmd = [cxx, "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-           "-fno-fast-math", str(src), "-o", str(LIB_PATH)]
+    fp = ["-ffp-contract=fast"] + _native_flags() if native else ["-ffp-contract=off"]
+    cmd = [cxx, "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-fno-fast-math"] + fp + \
+          [str(src), "-o", str(out)]
     subprocess.run(cmd, check=True)
-    return LIB_PATH
+    return out
 
 
-_lib = None
+_libs: dict = {}
 
 
-def lib() -> ctypes.CDLL:
-    global _lib
-    if _lib is None:
-        if not LIB_PATH.exists():
-            build()
-        L = ctypes.CDLL(str(LIB_PATH))
+def lib(native: bool = False) -> ctypes.CDLL:
+    """The parity build (default) or the native timing build of the oracle."""
+    if native not in _libs:
+        path = NATIVE_LIB_PATH if native else LIB_PATH
+        if not path.exists():
+            build(native=native)
+        L = ctypes.CDLL(str(path))
         P = ctypes.c_void_p
         for sfx in ("f32", "f64", "pert_f32"):
             getattr(L, f"oracle_init_{sfx}").argtypes = [P, P, P]
@@ -89,8 +105,8 @@ def lib() -> ctypes.CDLL:
         L.oracle_render.argtypes = [P, P] + [ctypes.c_int] * 6 + [P]
         L.oracle_f32_to_f16.argtypes = [ctypes.c_float]
         L.oracle_f32_to_f16.restype = ctypes.c_uint16
-        _lib = L
-    return _lib
+        _libs[native] = L
+    return _libs[native]
 
 
 _libm = ctypes.CDLL("libm.so.6")
@@ -340,14 +356,16 @@ class OracleSim:
     """CPU restatement of `Simulation` (src/gpu/sim.rs:180-1026)."""
 
     def __init__(self, grid, model: dict | None = None, schedule=None, precision: str = "f32",
-                 eos: tuple = ("bag", 1.0, 0.0)):
+                 eos: tuple = ("bag", 1.0, 0.0), native: bool = False):
         """precision: "f32", "f64", "mixed" (FP32 with the primitive recovery
         redone in FP64 where v^2 > 8/9, include/bubble.h
         BUBBLE_PRECISION_MIXED) or "pert" (the MIXED form with the fluid
         energy stored as E - e_ref, BUBBLE_PRECISION_PERTURBATION).
         eos: ("bag", -, -), ("bag_dof", ratio, -), ("gamma_law", Gamma, e0) or
         ("thermal", gamma, A) (include/bubble.h BUBBLE_EOS_*; the gamma law and
-        the thermal potential in FP32 only)."""
+        the thermal potential in FP32 only).  native: run on the native timing
+        build of the oracle (the CPU baseline) instead of the parity build."""
+        self.L = lib(native)
         self.eos = (eos[0], f32(eos[1]), f32(eos[2]))
         self.gamma = eos[0] == "gamma_law"
         self.thermal = eos[0] == "thermal"
@@ -387,7 +405,7 @@ class OracleSim:
         self.next_event = 0
         if schedule is not None:
             self.schedule = list(schedule)
-        getattr(lib(), f"oracle_init_{self.ksfx}")(_ptr(self.P), _ptr(self.field[0]), _ptr(self.fluid[0]))
+        getattr(self.L, f"oracle_init_{self.ksfx}")(_ptr(self.P), _ptr(self.field[0]), _ptr(self.fluid[0]))
 
     def set_state(self, field: np.ndarray, fluid: np.ndarray):
         self.field[self.cur] = field.reshape(self.n, 2)
@@ -398,7 +416,7 @@ class OracleSim:
 
     def nucleate(self, bubbles: np.ndarray):
         b = np.ascontiguousarray(bubbles, dtype=np.float32).reshape(-1, 4)
-        getattr(lib(), f"oracle_nucleate_{self.sfx}")(_ptr(self.P), _ptr(b), len(b), _ptr(self.field[self.cur]))
+        getattr(self.L, f"oracle_nucleate_{self.sfx}")(_ptr(self.P), _ptr(b), len(b), _ptr(self.field[self.cur]))
 
     # record_nucleation (src/gpu/sim.rs:843-879)
     def record_nucleation(self):
@@ -412,7 +430,7 @@ class OracleSim:
             self.nucleate(np.array(batch, dtype=np.float32))
 
     def stage(self, stage: int, in_slot: int, out_slot: int):
-        L = lib()
+        L = self.L
         self._set_eos()
         a0, a1 = (RK3_F32 if self.dtype == np.float32 else RK3_F64)[stage]
         S = np.array([a0, a1, self.d["dt"], 0.0], dtype=self.dtype)
@@ -428,9 +446,9 @@ class OracleSim:
         c2 = f32(a - f32(1.0)) if kind == "gamma_law" else f32(0.0)
         e0 = b if kind == "gamma_law" else f32(0.0)
         dof = a if kind == "bag_dof" else f32(1.0)
-        lib().oracle_set_eos(float(c2), float(e0), float(dof))
+        self.L.oracle_set_eos(float(c2), float(e0), float(dof))
         if kind == "thermal":
-            lib().oracle_set_thermal(*[float(x) for x in thermal_constants(self.d["a_rad"], a, b)])
+            self.L.oracle_set_thermal(*[float(x) for x in thermal_constants(self.d["a_rad"], a, b)])
 
     # record_step (src/gpu/sim.rs:881-916)
     def record_step(self):
@@ -458,7 +476,7 @@ class OracleSim:
     def visualise(self) -> np.ndarray:
         """The vis texture of the current slot as (nz, ny, nx, 4) uint16
         (binary16 bits of phi/phi_b, |v|, T/T_ref - 1, (E+p)v^2/e_ref)."""
-        L = lib()
+        L = self.L
         self._set_eos()
         getattr(L, f"oracle_primitives_{self.psfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
                                                     _ptr(self.fluid[self.cur]), _ptr(self.prim))
@@ -470,7 +488,7 @@ class OracleSim:
 
     # record_visualisation's primitives pass + reduce (src/gpu/sim.rs:918-1010)
     def diagnostics(self) -> dict:
-        L = lib()
+        L = self.L
         self._set_eos()
         getattr(L, f"oracle_primitives_{self.psfx}")(_ptr(self.P), _ptr(self.field[self.cur]),
                                                     _ptr(self.fluid[self.cur]), _ptr(self.prim))
