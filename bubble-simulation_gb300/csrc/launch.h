@@ -64,6 +64,15 @@ cudaError_t stage_v2_f32_fast(const StageArgs<float> &A, const LatticeParams<flo
 cudaError_t stage_v2_f64(const StageArgs<double> &A, const LatticeParams<double> &P, TileShape shape,
                          const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
 
+// ---- fused stage kernel, column form (stage_v3.cuh): same arguments ------
+size_t v3_smem_bytes(int precision_double, int ty);
+cudaError_t stage_v3_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
+                                int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
+cudaError_t stage_v3_f32_fast(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
+                              int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
+cudaError_t stage_v3_f64(const StageArgs<double> &A, const LatticeParams<double> &P, TileShape shape,
+                         const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
+
 }  // namespace launch
 }  // namespace bubble
 

@@ -426,7 +426,7 @@ int Simulation::stage_launch(int stage, uint32_t in_slot, uint32_t out_slot, std
     const uint64_t n = n_cells_;
     cudaError_t e = cudaSuccess;
     const int mode = arith_mode();
-    if (mode != 0 && path_ != KernelPath::Fused) {
+    if (mode != 0 && path_ == KernelPath::Reference) {
         err = "the MIXED and perturbation forms and the gamma-law and thermal equations of state run on the "
               "default (fused) kernel path only";
         return BUBBLE_ERR_INVALID;
@@ -451,8 +451,11 @@ int Simulation::stage_launch(int stage, uint32_t in_slot, uint32_t out_slot, std
             e = launch::prim_f64(A.fluid_in, (V4<double> *)prim_, n, P, stream_);
             if (e == cudaSuccess) e = launch::stage_ref_f64(A, (const V4<double> *)prim_, P, stream_);
             launches_ += 2;
-        } else {
+        } else if (path_ == KernelPath::FusedV2) {
             e = launch::stage_v2_f64(A, P, tile_, maps_[in_slot], tma_ok_ ? 1 : 0, d_status_, stream_);
+            launches_ += 1;
+        } else {
+            e = launch::stage_v3_f64(A, P, tile_, maps_[in_slot], tma_ok_ ? 1 : 0, d_status_, stream_);
             launches_ += 1;
         }
     } else {
@@ -474,12 +477,19 @@ int Simulation::stage_launch(int stage, uint32_t in_slot, uint32_t out_slot, std
             e = launch::prim_f32(A.fluid_in, (V4<float> *)prim_, n, P, stream_);
             if (e == cudaSuccess) e = launch::stage_ref_f32(A, (const V4<float> *)prim_, P, stream_);
             launches_ += 2;
-        } else {
+        } else if (path_ == KernelPath::FusedV2) {
             const int tma = tma_ok_ ? 1 : 0;
             if (spec_.math == BUBBLE_MATH_STRICT)
                 e = launch::stage_v2_f32_strict(A, P, tile_, mode, maps_[in_slot], tma, d_status_, stream_);
             else
                 e = launch::stage_v2_f32_fast(A, P, tile_, mode, maps_[in_slot], tma, d_status_, stream_);
+            launches_ += 1;
+        } else {
+            const int tma = tma_ok_ ? 1 : 0;
+            if (spec_.math == BUBBLE_MATH_STRICT)
+                e = launch::stage_v3_f32_strict(A, P, tile_, mode, maps_[in_slot], tma, d_status_, stream_);
+            else
+                e = launch::stage_v3_f32_fast(A, P, tile_, mode, maps_[in_slot], tma, d_status_, stream_);
             launches_ += 1;
         }
     }
