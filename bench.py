@@ -678,7 +678,7 @@ def main() -> int:
                 "frac": achieved / peak, "peak_kind": peak_kind,
                 "traffic": (traffic_per_cell * cells / 3) if traffic_per_cell else None,
                 "algorithmic_bytes_per_launch": BYTES_PER_CELL_UPDATE * cells / 3,
-                "kernel": "stage_v2_kernel (3 launches per step)"}
+                "kernel": "stage_kernel (3 launches per step)"}
     flop_per_cell = ncu_flops()
     fp32 = None
     if flop_per_cell:

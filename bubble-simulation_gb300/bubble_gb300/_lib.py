@@ -30,7 +30,7 @@ MATH = {"fast": 0, "strict": 1}
 EOS = {"bag": 0, "bag_dof": 1, "gamma_law": 2, "thermal": 3}
 PATH_FUSED = 0
 PATH_REFERENCE = 1
-PATHS = {"fused": PATH_FUSED, "reference": PATH_REFERENCE, "fused_v2": 2}
+PATHS = {"fused": PATH_FUSED, "reference": PATH_REFERENCE}
 MIN_GRID = 8
 MAX_GRID = 2048
 MAX_BATCH = 1024

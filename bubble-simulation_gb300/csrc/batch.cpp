@@ -593,8 +593,8 @@ int Batch::launch_solo(Lat &L, uint64_t k, std::string &err) {
             const TileShape tile{32, ty_, L.lz};
             const int tma = L.tma_ok ? 1 : 0;
             const cudaError_t e =
-                fast_ ? launch::stage_v3_f32_fast(A, L.P, tile, 0, L.maps[in[st]], tma, d_status_, stream_)
-                      : launch::stage_v3_f32_strict(A, L.P, tile, 0, L.maps[in[st]], tma, d_status_, stream_);
+                fast_ ? launch::stage_f32_fast(A, L.P, tile, 0, L.maps[in[st]], tma, d_status_, stream_)
+                      : launch::stage_f32_strict(A, L.P, tile, 0, L.maps[in[st]], tma, d_status_, stream_);
             BATCH_CUDA(e, "stage kernel of a solo lattice");
             ++launches_;
         }

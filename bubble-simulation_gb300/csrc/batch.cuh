@@ -12,7 +12,7 @@
 #pragma once
 
 #include "batch_desc.h"
-#include "stage_v3.cuh"
+#include "stage_column.cuh"
 
 namespace bubble {
 namespace dev {
@@ -59,8 +59,8 @@ BUBBLE_DEV bool grid_barrier(unsigned int *count, unsigned int *gen, int *status
 // sync: counters[0] = barrier count, counters[1] = barrier generation,
 //       counters[2] = work counter (zeroed before the launch).
 template <bool FAST, int TY>
-__global__ void __launch_bounds__(V3Layout<float, TY>::NT, V3Layout<float, TY>::MIN_BLOCKS)
-    batch_v2_kernel(const BatchLattice *__restrict__ lat, int n_lat, int n_items, int steps,
+__global__ void __launch_bounds__(ColumnLayout<float, TY>::NT, ColumnLayout<float, TY>::MIN_BLOCKS)
+    batch_kernel(const BatchLattice *__restrict__ lat, int n_lat, int n_items, int steps,
                     unsigned int *counters, int *status, unsigned int barrier_extra, int barrier_shift) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int item_s;
@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(V3Layout<float, TY>::NT, V3Layout<float, TY>::
                 A.dt = B.dt;
                 A.stage = stage;
                 const LatticeParams<float> P = B.P;
-                if (!v3_item<float, FAST, kPlain, TY>(smem, A, P, B.lz, &B.maps[in_slot], B.tma_ok, status,
+                if (!column_item<float, FAST, kPlain, TY>(smem, A, P, B.lz, &B.maps[in_slot], B.tma_ok, status,
                                                       local % B.tiles_xy, local / B.tiles_xy)) {
                     // record where the stage's bounded wait gave up (status[8..12])
                     if (threadIdx.x == 0 && atomicCAS(&status[8], 0, 1) == 0) {

@@ -287,7 +287,7 @@ int bubble_load_state_f64(bubble_sim *sim, const double *field, const double *fl
 // ---------------------------------------------------------------------------
 int bubble_ext_set_path(bubble_sim *sim, int32_t path) {
     if (!sim || !sim->impl) return fail(BUBBLE_ERR_INVALID, "sim is NULL");
-    if (path != BUBBLE_PATH_FUSED && path != BUBBLE_PATH_REFERENCE && path != 2)
+    if (path != BUBBLE_PATH_FUSED && path != BUBBLE_PATH_REFERENCE)
         return fail(BUBBLE_ERR_INVALID, "unknown kernel path");
     sim->impl->set_path(static_cast<bubble::KernelPath>(path));
     return BUBBLE_OK;

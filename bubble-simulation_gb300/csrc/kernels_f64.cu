@@ -36,18 +36,12 @@ cudaError_t diag_f64(const V2<double> *field, const V4<double> *fluid,
 namespace bubble {
 namespace launch {
 
-cudaError_t stage_v2_f64(const StageArgs<double> &A, const LatticeParams<double> &P, TileShape shape,
-                         const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
-    using namespace launch_detail;
-    if (shape.tx != 32 || shape.ty != 4) return cudaErrorInvalidValue;
-    return stage_v2<double, false, false, 4>(A, P, shape.lz, maps, tma_ok, status, s);
-}
 
-cudaError_t stage_v3_f64(const StageArgs<double> &A, const LatticeParams<double> &P, TileShape shape,
+cudaError_t stage_f64(const StageArgs<double> &A, const LatticeParams<double> &P, TileShape shape,
                          const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
     using namespace launch_detail;
     if (shape.tx != 32 || shape.ty != 4) return cudaErrorInvalidValue;
-    return stage_v3<double, false, false, 4>(A, P, shape.lz, maps, tma_ok, status, s);
+    return stage_column<double, false, false, 4>(A, P, shape.lz, maps, tma_ok, status, s);
 }
 
 }  // namespace launch

@@ -5,40 +5,22 @@
 namespace bubble {
 namespace launch {
 
-cudaError_t stage_v2_f32_fast(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
-                              int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
-    using namespace launch_detail;
-    if (shape.tx != 32) return cudaErrorInvalidValue;
-    if (shape.ty == 8) {
-        if (mode == dev::kThermal)
-            return stage_v2<float, true, dev::kThermal, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-        if (mode == dev::kGamma) return stage_v2<float, true, dev::kGamma, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-        if (mode == dev::kPert) return stage_v2<float, true, dev::kPert, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-        if (mode == dev::kMixed) return stage_v2<float, true, dev::kMixed, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-        return stage_v2<float, true, dev::kPlain, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-    }
-    if (shape.ty == 4 && (mode == dev::kPlain || mode == dev::kMixed)) {
-        if (mode == dev::kMixed) return stage_v2<float, true, dev::kMixed, 4>(A, P, shape.lz, maps, tma_ok, status, s);
-        return stage_v2<float, true, dev::kPlain, 4>(A, P, shape.lz, maps, tma_ok, status, s);
-    }
-    return cudaErrorInvalidValue;
-}
 
-cudaError_t stage_v3_f32_fast(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
+cudaError_t stage_f32_fast(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
                               int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
     using namespace launch_detail;
     if (shape.tx != 32) return cudaErrorInvalidValue;
     if (shape.ty == 8) {
         if (mode == dev::kThermal)
-            return stage_v3<float, true, dev::kThermal, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-        if (mode == dev::kGamma) return stage_v3<float, true, dev::kGamma, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-        if (mode == dev::kPert) return stage_v3<float, true, dev::kPert, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-        if (mode == dev::kMixed) return stage_v3<float, true, dev::kMixed, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-        return stage_v3<float, true, dev::kPlain, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+            return stage_column<float, true, dev::kThermal, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+        if (mode == dev::kGamma) return stage_column<float, true, dev::kGamma, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+        if (mode == dev::kPert) return stage_column<float, true, dev::kPert, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+        if (mode == dev::kMixed) return stage_column<float, true, dev::kMixed, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+        return stage_column<float, true, dev::kPlain, 8>(A, P, shape.lz, maps, tma_ok, status, s);
     }
     if (shape.ty == 4 && (mode == dev::kPlain || mode == dev::kMixed)) {
-        if (mode == dev::kMixed) return stage_v3<float, true, dev::kMixed, 4>(A, P, shape.lz, maps, tma_ok, status, s);
-        return stage_v3<float, true, dev::kPlain, 4>(A, P, shape.lz, maps, tma_ok, status, s);
+        if (mode == dev::kMixed) return stage_column<float, true, dev::kMixed, 4>(A, P, shape.lz, maps, tma_ok, status, s);
+        return stage_column<float, true, dev::kPlain, 4>(A, P, shape.lz, maps, tma_ok, status, s);
     }
     return cudaErrorInvalidValue;
 }
@@ -56,7 +38,7 @@ int batch_max_grid(bool fast, int ty) {
     return 0;
 }
 size_t batch_smem_bytes(int ty) {
-    return ty == 4 ? dev::V3Layout<float, 4>::bytes : dev::V3Layout<float, 8>::bytes;
+    return ty == 4 ? dev::ColumnLayout<float, 4>::bytes : dev::ColumnLayout<float, 8>::bytes;
 }
 cudaError_t batch_launch(bool fast, int ty, const void *lat, int n_lat, int n_items, int steps,
                          unsigned int *counters, int *status, int grid, unsigned int barrier_extra,

@@ -45,39 +45,24 @@ int diag_blocks_for(uint64_t cells) { return dev::diag_blocks(cells); }
 namespace bubble {
 namespace launch {
 
-bool v2_shape_supported(int precision_double, int ty) {
+bool stage_shape_supported(int precision_double, int ty) {
     return precision_double ? ty == 4 : (ty == 4 || ty == 8);
 }
-size_t v3_smem_bytes(int precision_double, int ty) {
-    if (precision_double) return dev::V3Layout<double, 4>::bytes;
-    return ty == 4 ? dev::V3Layout<float, 4>::bytes : dev::V3Layout<float, 8>::bytes;
-}
-size_t v2_smem_bytes(int precision_double, int ty) {
-    if (precision_double) return dev::V2Layout<double, 4>::bytes;
-    return ty == 4 ? dev::V2Layout<float, 4>::bytes : dev::V2Layout<float, 8>::bytes;
-}
-cudaError_t stage_v2_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
-                                int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
-    using namespace launch_detail;
-    if (shape.tx != 32 || shape.ty != 8) return cudaErrorInvalidValue;
-    if (mode == dev::kThermal)
-        return stage_v2<float, false, dev::kThermal, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-    if (mode == dev::kGamma) return stage_v2<float, false, dev::kGamma, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-    if (mode == dev::kPert) return stage_v2<float, false, dev::kPert, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-    if (mode == dev::kMixed) return stage_v2<float, false, dev::kMixed, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-    return stage_v2<float, false, dev::kPlain, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+size_t stage_smem_bytes(int precision_double, int ty) {
+    if (precision_double) return dev::ColumnLayout<double, 4>::bytes;
+    return ty == 4 ? dev::ColumnLayout<float, 4>::bytes : dev::ColumnLayout<float, 8>::bytes;
 }
 
-cudaError_t stage_v3_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
+cudaError_t stage_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
                                 int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
     using namespace launch_detail;
     if (shape.tx != 32 || shape.ty != 8) return cudaErrorInvalidValue;
     if (mode == dev::kThermal)
-        return stage_v3<float, false, dev::kThermal, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-    if (mode == dev::kGamma) return stage_v3<float, false, dev::kGamma, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-    if (mode == dev::kPert) return stage_v3<float, false, dev::kPert, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-    if (mode == dev::kMixed) return stage_v3<float, false, dev::kMixed, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-    return stage_v3<float, false, dev::kPlain, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+        return stage_column<float, false, dev::kThermal, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+    if (mode == dev::kGamma) return stage_column<float, false, dev::kGamma, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+    if (mode == dev::kPert) return stage_column<float, false, dev::kPert, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+    if (mode == dev::kMixed) return stage_column<float, false, dev::kMixed, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+    return stage_column<float, false, dev::kPlain, 8>(A, P, shape.lz, maps, tma_ok, status, s);
 }
 
 }  // namespace launch

@@ -50,27 +50,19 @@ cudaError_t diag_f64(const V2<double> *field, const V4<double> *fluid,
 size_t diag_partials_bytes();
 int diag_blocks_for(uint64_t cells);
 
-// ---- fused stage kernel with asynchronous (TMA / cp.async) staging --------
+// ---- fused stage kernel, column form (stage_column.cuh) -----------------------
 // `maps` are the tensor maps of the stage input slot (tma.h); `tma_ok` says
 // whether they are valid; bit 0 of *status is set if a bounded wait expired.
-bool v2_shape_supported(int precision_double, int ty);
-size_t v2_smem_bytes(int precision_double, int ty);
-// `mode` as for diag_f32; the perturbation and gamma-law forms are built for
-// ty = 8 only.
-cudaError_t stage_v2_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
+// Tile heights: 4 or 8 in FP32, 4 in FP64.  `mode`: 0 plain, 1 mixed, 2
+// perturbation form, 3 gamma-law equation of state, 4 thermal potential; the
+// last three and the strict arithmetic are built for ty = 8 only.
+bool stage_shape_supported(int precision_double, int ty);
+size_t stage_smem_bytes(int precision_double, int ty);
+cudaError_t stage_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
                                 int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
-cudaError_t stage_v2_f32_fast(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
+cudaError_t stage_f32_fast(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
                               int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
-cudaError_t stage_v2_f64(const StageArgs<double> &A, const LatticeParams<double> &P, TileShape shape,
-                         const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
-
-// ---- fused stage kernel, column form (stage_v3.cuh): same arguments ------
-size_t v3_smem_bytes(int precision_double, int ty);
-cudaError_t stage_v3_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
-                                int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
-cudaError_t stage_v3_f32_fast(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
-                              int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
-cudaError_t stage_v3_f64(const StageArgs<double> &A, const LatticeParams<double> &P, TileShape shape,
+cudaError_t stage_f64(const StageArgs<double> &A, const LatticeParams<double> &P, TileShape shape,
                          const StageMaps &maps, int tma_ok, int *status, cudaStream_t s);
 
 }  // namespace launch

@@ -9,8 +9,7 @@
 
 #include "kernels.cuh"
 #include "launch.h"
-#include "stage_v2.cuh"
-#include "stage_v3.cuh"
+#include "stage_column.cuh"
 
 namespace bubble {
 namespace launch_detail {
@@ -85,26 +84,11 @@ cudaError_t stage_ref(const StageArgs<R> &A, const V4<R> *prim, const LatticePar
     return cudaGetLastError();
 }
 
-template <typename R, bool FAST, int MIXED, int TY>
-cudaError_t stage_v2(const StageArgs<R> &A, const LatticeParams<R> &P, int lz, const StageMaps &maps, int tma_ok,
-                     int *status, cudaStream_t s) {
-    using L = dev::V2Layout<R, TY>;
-    auto k = dev::stage_v2_kernel<R, FAST, MIXED, TY>;
-    cudaError_t e = ensure_smem(k, L::bytes);
-    if (e != cudaSuccess) return e;
-    if (lz < 1) lz = 1;
-    const int ntx = (P.nx + L::TX - 1) / L::TX, nty = (P.ny + TY - 1) / TY;
-    const int nzc = (P.nz + lz - 1) / lz;
-    dim3 grid(ntx * nty, nzc);
-    k<<<grid, L::NT, L::bytes, s>>>(A, P, lz, maps, tma_ok, status);
-    return cudaGetLastError();
-}
-
 template <typename R, bool FAST, int FORM, int TY>
-cudaError_t stage_v3(const StageArgs<R> &A, const LatticeParams<R> &P, int lz, const StageMaps &maps, int tma_ok,
+cudaError_t stage_column(const StageArgs<R> &A, const LatticeParams<R> &P, int lz, const StageMaps &maps, int tma_ok,
                      int *status, cudaStream_t s) {
-    using L = dev::V3Layout<R, TY>;
-    auto k = dev::stage_v3_kernel<R, FAST, FORM, TY>;
+    using L = dev::ColumnLayout<R, TY>;
+    auto k = dev::stage_kernel<R, FAST, FORM, TY>;
     cudaError_t e = ensure_smem(k, L::bytes);
     if (e != cudaSuccess) return e;
     if (lz < 1) lz = 1;
@@ -135,8 +119,8 @@ namespace launch_detail {
 
 template <bool FAST, int TY>
 int batch_max_grid() {
-    using L = dev::V3Layout<float, TY>;
-    auto k = dev::batch_v2_kernel<FAST, TY>;
+    using L = dev::ColumnLayout<float, TY>;
+    auto k = dev::batch_kernel<FAST, TY>;
     if (ensure_smem(k, L::bytes) != cudaSuccess) return 0;
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
@@ -148,8 +132,8 @@ int batch_max_grid() {
 template <bool FAST, int TY>
 cudaError_t batch_launch(const void *lat, int n_lat, int n_items, int steps, unsigned int *counters,
                          int *status, int grid, unsigned int barrier_extra, int barrier_shift, cudaStream_t s) {
-    using L = dev::V3Layout<float, TY>;
-    auto k = dev::batch_v2_kernel<FAST, TY>;
+    using L = dev::ColumnLayout<float, TY>;
+    auto k = dev::batch_kernel<FAST, TY>;
     cudaError_t e = ensure_smem(k, L::bytes);
     if (e != cudaSuccess) return e;
     const BatchLattice *lp = static_cast<const BatchLattice *>(lat);

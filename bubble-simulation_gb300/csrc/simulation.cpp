@@ -356,7 +356,7 @@ int Simulation::set_tile(TileShape t, std::string &err) {
                       spec_.eos == BUBBLE_EOS_THERMAL;
     // the synchronous-staging and strict kernels are built for fewer shapes
     // than the default one; their launches check the shape themselves
-    if (t.tx != 32 || !launch::v2_shape_supported(is_f64(), t.ty) || ((strict || pert) && t.ty != 8) || t.lz < 1) {
+    if (t.tx != 32 || !launch::stage_shape_supported(is_f64(), t.ty) || ((strict || pert) && t.ty != 8) || t.lz < 1) {
         err = "unsupported tile shape";
         return BUBBLE_ERR_INVALID;
     }
@@ -451,11 +451,8 @@ int Simulation::stage_launch(int stage, uint32_t in_slot, uint32_t out_slot, std
             e = launch::prim_f64(A.fluid_in, (V4<double> *)prim_, n, P, stream_);
             if (e == cudaSuccess) e = launch::stage_ref_f64(A, (const V4<double> *)prim_, P, stream_);
             launches_ += 2;
-        } else if (path_ == KernelPath::FusedV2) {
-            e = launch::stage_v2_f64(A, P, tile_, maps_[in_slot], tma_ok_ ? 1 : 0, d_status_, stream_);
-            launches_ += 1;
         } else {
-            e = launch::stage_v3_f64(A, P, tile_, maps_[in_slot], tma_ok_ ? 1 : 0, d_status_, stream_);
+            e = launch::stage_f64(A, P, tile_, maps_[in_slot], tma_ok_ ? 1 : 0, d_status_, stream_);
             launches_ += 1;
         }
     } else {
@@ -477,19 +474,12 @@ int Simulation::stage_launch(int stage, uint32_t in_slot, uint32_t out_slot, std
             e = launch::prim_f32(A.fluid_in, (V4<float> *)prim_, n, P, stream_);
             if (e == cudaSuccess) e = launch::stage_ref_f32(A, (const V4<float> *)prim_, P, stream_);
             launches_ += 2;
-        } else if (path_ == KernelPath::FusedV2) {
-            const int tma = tma_ok_ ? 1 : 0;
-            if (spec_.math == BUBBLE_MATH_STRICT)
-                e = launch::stage_v2_f32_strict(A, P, tile_, mode, maps_[in_slot], tma, d_status_, stream_);
-            else
-                e = launch::stage_v2_f32_fast(A, P, tile_, mode, maps_[in_slot], tma, d_status_, stream_);
-            launches_ += 1;
         } else {
             const int tma = tma_ok_ ? 1 : 0;
             if (spec_.math == BUBBLE_MATH_STRICT)
-                e = launch::stage_v3_f32_strict(A, P, tile_, mode, maps_[in_slot], tma, d_status_, stream_);
+                e = launch::stage_f32_strict(A, P, tile_, mode, maps_[in_slot], tma, d_status_, stream_);
             else
-                e = launch::stage_v3_f32_fast(A, P, tile_, mode, maps_[in_slot], tma, d_status_, stream_);
+                e = launch::stage_f32_fast(A, P, tile_, mode, maps_[in_slot], tma, d_status_, stream_);
             launches_ += 1;
         }
     }

@@ -28,7 +28,6 @@ namespace bubble {
 enum class KernelPath : int {
     Fused = 0,      // one fused launch per RK stage with async staging (default)
     Reference = 1,  // primitives pass + stage pass per RK stage, as in the reference
-    FusedV2 = 2,    // the item-plan fused kernel (stage_v2.cuh)
 };
 
 class Simulation {

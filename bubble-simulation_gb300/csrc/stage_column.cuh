@@ -42,7 +42,7 @@ namespace bubble {
 namespace dev {
 
 template <typename R, int TY>
-struct V3Layout {
+struct ColumnLayout {
     static constexpr int TX = 32;
     static constexpr int PW = TX + 4, PH = TY + 4, PC = PW * PH, NC = TX * TY;
     static constexpr int NH = 64;  // halo threads: two warps
@@ -172,9 +172,9 @@ BUBBLE_DEV void combine_cell(const StageArgs<R> &A, const LatticeParams<R> &P, s
 // stop.  Usable repeatedly by one CTA: it starts with a barrier and leaves
 // no copy in flight.
 template <typename R, bool FAST, int FORM, int TY>
-BUBBLE_DEV bool v3_item(unsigned char *smem, const StageArgs<R> &A, const LatticeParams<R> &P, int lz,
+BUBBLE_DEV bool column_item(unsigned char *smem, const StageArgs<R> &A, const LatticeParams<R> &P, int lz,
                         const StageMaps *maps, int tma_ok, int *status, int tile_xy, int chunk) {
-    using L = V3Layout<R, TY>;
+    using L = ColumnLayout<R, TY>;
     constexpr int TX = L::TX, NC = L::NC, NH = L::NH, PW = L::PW, PC = L::PC;
     __syncthreads();  // a previous item on this CTA is done with shared memory
     V4<R> *raw_u = reinterpret_cast<V4<R> *>(smem + L::o_rawu);
@@ -475,11 +475,11 @@ BUBBLE_DEV bool v3_item(unsigned char *smem, const StageArgs<R> &A, const Lattic
 }
 
 template <typename R, bool FAST, int FORM, int TY>
-__global__ void __launch_bounds__(V3Layout<R, TY>::NT, V3Layout<R, TY>::MIN_BLOCKS)
-    stage_v3_kernel(StageArgs<R> A, LatticeParams<R> P, int lz, const __grid_constant__ StageMaps maps,
+__global__ void __launch_bounds__(ColumnLayout<R, TY>::NT, ColumnLayout<R, TY>::MIN_BLOCKS)
+    stage_kernel(StageArgs<R> A, LatticeParams<R> P, int lz, const __grid_constant__ StageMaps maps,
                     int tma_ok, int *status) {
     extern __shared__ __align__(128) unsigned char smem[];
-    v3_item<R, FAST, FORM, TY>(smem, A, P, lz, &maps, tma_ok, status, blockIdx.x, blockIdx.y);
+    column_item<R, FAST, FORM, TY>(smem, A, P, lz, &maps, tma_ok, status, blockIdx.x, blockIdx.y);
 }
 
 }  // namespace dev
