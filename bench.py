@@ -1,7 +1,7 @@
 """Benchmark of the GB300 lattice time step.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload precision512|default128|plain64|profile256|batch64|serve|precision_study]
+                    [--workload precision512|default128|plain64|profile256|batch64|serve|serve_light|precision_study]
 
 Metric: cell-updates/s (one cell-update = one full SSP-RK3 step of one
 cell), on the 512^3 precision-study workload by default: periodic 512^3
@@ -384,9 +384,9 @@ def run_batch(args) -> int:
     broken_p = []
     for s in specs:
         if s.grid not in lz_cache:
-            lz_cache[s.grid] = bubble.autotune_chunk(s.grid, 8, "fast")
+            lz_cache[s.grid] = bubble.autotune_chunk(s.grid, 16, "fast")
         sim = bubble.Simulation(s)
-        sim.set_tile(8, lz_cache[s.grid])
+        sim.set_tile(16, lz_cache[s.grid])
         sim.synchronize()
         t0 = time.perf_counter()
         sim.advance(steps)
@@ -408,7 +408,10 @@ def run_batch(args) -> int:
     return 0
 
 
-def serve_requests(bubble, n: int, seed: int = 20251203):
+SERVE_EDGES = {"serve": (48, 64, 128, 192, 256), "serve_light": (48, 64, 96, 128)}
+
+
+def serve_requests(bubble, n: int, seed: int = 20251203, edges=SERVE_EDGES["serve"]):
     """The serving workload: edges from {48, 64, 128, 192, 256}, 1-32 bubbles
     with nucleation times uniform over the first 200 steps, eta log-U[0.02, 1],
     seed factor U[0.9, 1.5], 500-3000 steps; Poisson arrivals at 20 req/s."""
@@ -416,7 +419,7 @@ def serve_requests(bubble, n: int, seed: int = 20251203):
     reqs, t = [], 0.0
     for k in range(n):
         t += float(rng.exponential(1.0 / 20.0))
-        edge = int(rng.choice([48, 64, 128, 192, 256]))
+        edge = int(rng.choice(list(edges)))
         model = bubble.Model(eta=float(math.exp(rng.uniform(math.log(0.02), math.log(1.0)))),
                              seed_value=float(rng.uniform(0.9, 1.5)))
         spec = bubble.SimulationSpec(model=model, grid=(edge,) * 3, nucleation="uniform",
@@ -441,7 +444,8 @@ def run_serve(args) -> int:
     import bubble_gb300 as bubble
 
     bubble.load()
-    reqs = serve_requests(bubble, args.requests)
+    edges = SERVE_EDGES[args.workload]
+    reqs = serve_requests(bubble, args.requests, edges=edges)
     n = len(reqs)
 
     def serve(policy):
@@ -483,10 +487,23 @@ def run_serve(args) -> int:
         plain_lat.append(free_at - arr)
         finish = free_at
     cells = sum(s.grid[0] ** 3 * k for _, s, k in reqs)
+    # The bound on any schedule of these requests: every cell-update at the
+    # fastest rate the plain path reaches on any one of them (its largest
+    # lattices fill the GPU alone); the plain path's busy time over that.
+    work = [s.grid[0] ** 3 * k for _, s, k in reqs]
+    rates = [w / d for w, d in zip(work, durations)]
+    r_max = max(rates)
+    per_edge = {}
+    for (_, s, _), r in zip(reqs, rates):
+        per_edge.setdefault(s.grid[0], []).append(r)
+    bound = {"fastest_plain_rate": r_max, "ratio_bound": sum(durations) / (sum(work) / r_max),
+             "plain_rate_by_edge": {str(e): sum(v) / len(v) for e, v in sorted(per_edge.items())}}
+    edge_txt = ",".join(str(e) for e in edges)
     line = {"metric": "solves/s", "value": n / span, "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
             "dtype": "f32", "data": "synthetic", "impl": "gb300-serve",
-            "config": {"workload": f"{n} requests, Poisson 20/s, edges from {{48,64,128,192,256}}, 1-32 bubbles, "
+            "config": {"workload": f"{n} requests, Poisson 20/s, edges from {{{edge_txt}}}, 1-32 bubbles, "
                                    "eta log-U[0.02,1], seed factor U[0.9,1.5], 500-3000 steps, FP32 fast"},
+            "speedup_vs_plain": (n / span) / (n / (finish - reqs[0][0])), "bound": bound,
             "p50_latency_s": percentile(lat, 0.5), "p99_latency_s": percentile(lat, 0.99),
             "cell_updates_per_s": cells / span, "policy": "fifo with backfill, 24 M resident cells", "chunk_planes": args.chunk_planes or 64,
             "shortest_first": {"solves_per_s": n / span_sj, "p50_latency_s": percentile(lat_sj, 0.5),
@@ -585,7 +602,7 @@ def main() -> int:
     args.warmup = max(args.warmup, 3)
     if args.workload == "batch64":
         return run_batch(args)
-    if args.workload == "serve":
+    if args.workload in SERVE_EDGES:
         return run_serve(args)
     if args.workload == "precision_study":
         return run_precision_study(args)

@@ -396,7 +396,7 @@ class Batch:
     """Many independent lattices advanced by one persistent, graph-captured
     launch per chunk of steps (include/bubble_batch.h)."""
 
-    def __init__(self, specs: list[SimulationSpec], tile_y: int = 8, autotune: bool = True,
+    def __init__(self, specs: list[SimulationSpec], tile_y: int = 16, autotune: bool = True,
                  use_graph: bool = True, max_grid: int = 0):
         self._L = load()
         self.specs = list(specs)
@@ -456,7 +456,7 @@ class Batch:
         return {n: getattr(i, n) for n, _ in _lib.BatchInfo._fields_}
 
 
-def autotune_chunk(grid, tile_y: int = 8, math: str = "fast") -> int:
+def autotune_chunk(grid, tile_y: int = 16, math: str = "fast") -> int:
     lz = ctypes.c_int32()
     check(load().bubble_autotune_chunk((ctypes.c_uint32 * 3)(*grid), tile_y, _lib.MATH[math], ctypes.byref(lz)))
     return lz.value
@@ -466,7 +466,7 @@ class Server:
     """Request loop with continuous batching (include/bubble_server.h)."""
 
     def __init__(self, math: str = "fast", chunk_steps: int = 50, max_active: int = 64,
-                 memory_fraction: float = 0.85, use_graph: bool = True, tile_y: int = 8,
+                 memory_fraction: float = 0.85, use_graph: bool = True, tile_y: int = 16,
                  resident_cells: int = 0, policy: str = "fifo", chunk_planes: int = 0):
         self._L = load()
         opt = _lib.ServerOptions(_lib.MATH[math], tile_y, chunk_steps, max_active, memory_fraction, int(use_graph),

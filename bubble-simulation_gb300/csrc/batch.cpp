@@ -106,7 +106,7 @@ int autotune_chunk(const uint32_t grid[3], int ty, bool fast, std::string &err) 
     // The quiescent initial state is an exact fixed point of the scheme, so
     // timing steps on it does not change the lattice.
     for (int lz : cand) {
-        if (sim->set_tile(TileShape{32, ty, lz}, err) != BUBBLE_OK) continue;
+        if (sim->set_tile(TileShape{tile_x_for(ty), ty, lz}, err) != BUBBLE_OK) continue;
         if (sim->record_steps(1, err) != BUBBLE_OK) break;
         cudaEventRecord(e0, sim->stream());
         if (sim->record_steps(3, err) != BUBBLE_OK) break;
@@ -131,7 +131,7 @@ int autotune_chunk(const uint32_t grid[3], int ty, bool fast, std::string &err) 
 // ---------------------------------------------------------------------------
 int Batch::setup(int math, const bubble_batch_options *opt, std::string &err) {
     bubble_batch_options o;
-    o.tile_y = 8;
+    o.tile_y = 16;
     o.autotune = 1;
     o.use_graph = 1;
     o.max_grid = 0;
@@ -142,8 +142,8 @@ int Batch::setup(int math, const bubble_batch_options *opt, std::string &err) {
         err = "unknown math mode";
         return BUBBLE_ERR_INVALID;
     }
-    if (o.tile_y != 8 && !(fast_ && o.tile_y == 4)) {
-        err = "batch tile_y must be 8 (or 4 in the fast mode)";
+    if (o.tile_y != 16 && !(fast_ && o.tile_y == 8)) {
+        err = "batch tile_y must be 16 (16 x 16 tiles; or 8, 32 x 8 tiles, in the fast mode)";
         return BUBBLE_ERR_INVALID;
     }
     ty_ = o.tile_y;
@@ -261,7 +261,7 @@ int Batch::allocate(Lat &L, std::string &err) {
         L.field[k] = static_cast<char *>(L.state) + k * slot;
         L.fluid[k] = static_cast<char *>(L.state) + k * slot + fb;
         L.tma_ok = L.tma_ok && encode_stage_maps(&L.maps[k], L.field[k], L.fluid[k], (int)L.grid[0],
-                                                 (int)L.grid[1], (int)L.grid[2], 32, ty_, 4);
+                                                 (int)L.grid[1], (int)L.grid[2], tile_x_for(ty_), ty_, 4);
     }
     BATCH_CUDA(launch::init_f32((V2<float> *)L.field[0], (V4<float> *)L.fluid[0], L.cells, L.P.e_ref, stream_),
                "init kernel");
@@ -288,7 +288,8 @@ int Batch::add(const bubble_spec &spec, uint32_t *index, std::string &err) {
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const long tiles = (long)((L.grid[0] + 31) / 32) * (long)((L.grid[1] + ty_ - 1) / ty_);
+        const long tx = tile_x_for(ty_);
+        const long tiles = (long)((L.grid[0] + tx - 1) / tx) * (long)((L.grid[1] + ty_ - 1) / ty_);
         L.solo = tiles * (((long)L.grid[2] + 31) / 32) >= 2L * std::max(sms, 1);
         if (L.solo) {
             L.lz = default_chunk(L.grid, ty_);
@@ -334,7 +335,8 @@ void Batch::plan_items() {
     n_items_ = 0;
     for (uint32_t k : item_order_) {
         const Lat &L = lats_[k];
-        const int tiles = (int)((L.grid[0] + 31) / 32) * (int)((L.grid[1] + ty_ - 1) / ty_);
+        const int tx = tile_x_for(ty_);
+        const int tiles = (int)((L.grid[0] + tx - 1) / tx) * (int)((L.grid[1] + ty_ - 1) / ty_);
         n_items_ += tiles * (int)((L.grid[2] + L.lz - 1) / L.lz);
     }
     grid_ = std::max(1, std::min(max_grid_, n_items_));
@@ -474,7 +476,7 @@ int Batch::launch_chunk(uint64_t k, std::string &err) {
         D.P = L.P;
         D.dt = L.dt;
         D.lz = L.lz;
-        D.tiles_xy = (int)((L.grid[0] + 31) / 32) * (int)((L.grid[1] + ty_ - 1) / ty_);
+        D.tiles_xy = (int)((L.grid[0] + tile_x_for(ty_) - 1) / tile_x_for(ty_)) * (int)((L.grid[1] + ty_ - 1) / ty_);
         D.chunks = (int)((L.grid[2] + L.lz - 1) / L.lz);
         D.item_begin = begin;
         D.cur0 = (int)L.cur;
@@ -590,7 +592,7 @@ int Batch::launch_solo(Lat &L, uint64_t k, std::string &err) {
             A.a1 = kRK3[st][1];
             A.dt = L.dt;
             A.stage = st;
-            const TileShape tile{32, ty_, L.lz};
+            const TileShape tile{tile_x_for(ty_), ty_, L.lz};
             const int tma = L.tma_ok ? 1 : 0;
             const cudaError_t e =
                 fast_ ? launch::stage_f32_fast(A, L.P, tile, 0, L.maps[in[st]], tma, d_status_, stream_)

@@ -22,7 +22,7 @@ extern "C" {
 
 void bubble_batch_options_default(bubble_batch_options *out) {
     if (!out) return;
-    out->tile_y = 8;
+    out->tile_y = 16;
     out->autotune = 1;
     out->use_graph = 1;
     out->max_grid = 0;

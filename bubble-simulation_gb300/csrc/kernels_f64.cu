@@ -38,10 +38,12 @@ namespace launch {
 
 
 cudaError_t stage_f64(const StageArgs<double> &A, const LatticeParams<double> &P, TileShape shape,
-                         const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
+                      const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
     using namespace launch_detail;
-    if (shape.tx != 32 || shape.ty != 4) return cudaErrorInvalidValue;
-    return stage_column<double, false, false, 4>(A, P, shape.lz, maps, tma_ok, status, s);
+    if (shape.tx != tile_x_for(shape.ty)) return cudaErrorInvalidValue;
+    if (shape.ty == 16) return stage_column<double, false, false, 16>(A, P, shape.lz, maps, tma_ok, status, s);
+    if (shape.ty == 4) return stage_column<double, false, false, 4>(A, P, shape.lz, maps, tma_ok, status, s);
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace launch

@@ -6,19 +6,23 @@ namespace bubble {
 namespace launch {
 
 
-cudaError_t stage_f32_fast(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
-                              int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
+cudaError_t stage_f32_fast(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape, int mode,
+                           const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
     using namespace launch_detail;
-    if (shape.tx != 32) return cudaErrorInvalidValue;
+    if (shape.tx != tile_x_for(shape.ty)) return cudaErrorInvalidValue;
+    if (shape.ty == 16) {
+        if (mode == dev::kThermal) return stage_column<float, true, dev::kThermal, 16>(A, P, shape.lz, maps, tma_ok, status, s);
+        if (mode == dev::kGamma) return stage_column<float, true, dev::kGamma, 16>(A, P, shape.lz, maps, tma_ok, status, s);
+        if (mode == dev::kPert) return stage_column<float, true, dev::kPert, 16>(A, P, shape.lz, maps, tma_ok, status, s);
+        if (mode == dev::kMixed) return stage_column<float, true, dev::kMixed, 16>(A, P, shape.lz, maps, tma_ok, status, s);
+        return stage_column<float, true, dev::kPlain, 16>(A, P, shape.lz, maps, tma_ok, status, s);
+    }
+    if (mode != dev::kPlain && mode != dev::kMixed) return cudaErrorInvalidValue;
     if (shape.ty == 8) {
-        if (mode == dev::kThermal)
-            return stage_column<float, true, dev::kThermal, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-        if (mode == dev::kGamma) return stage_column<float, true, dev::kGamma, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-        if (mode == dev::kPert) return stage_column<float, true, dev::kPert, 8>(A, P, shape.lz, maps, tma_ok, status, s);
         if (mode == dev::kMixed) return stage_column<float, true, dev::kMixed, 8>(A, P, shape.lz, maps, tma_ok, status, s);
         return stage_column<float, true, dev::kPlain, 8>(A, P, shape.lz, maps, tma_ok, status, s);
     }
-    if (shape.ty == 4 && (mode == dev::kPlain || mode == dev::kMixed)) {
+    if (shape.ty == 4) {
         if (mode == dev::kMixed) return stage_column<float, true, dev::kMixed, 4>(A, P, shape.lz, maps, tma_ok, status, s);
         return stage_column<float, true, dev::kPlain, 4>(A, P, shape.lz, maps, tma_ok, status, s);
     }
@@ -33,12 +37,12 @@ namespace launch {
 
 int batch_max_grid(bool fast, int ty) {
     if (!fast) return batch_max_grid_strict(ty);
+    if (ty == 16) return launch_detail::batch_max_grid<true, 16>();
     if (ty == 8) return launch_detail::batch_max_grid<true, 8>();
-    if (ty == 4) return launch_detail::batch_max_grid<true, 4>();
     return 0;
 }
 size_t batch_smem_bytes(int ty) {
-    return ty == 4 ? dev::ColumnLayout<float, 4>::bytes : dev::ColumnLayout<float, 8>::bytes;
+    return ty == 16 ? dev::ColumnLayout<float, 16>::bytes : dev::ColumnLayout<float, 8>::bytes;
 }
 cudaError_t batch_launch(bool fast, int ty, const void *lat, int n_lat, int n_items, int steps,
                          unsigned int *counters, int *status, int grid, unsigned int barrier_extra,
@@ -46,11 +50,11 @@ cudaError_t batch_launch(bool fast, int ty, const void *lat, int n_lat, int n_it
     if (!fast)
         return batch_launch_strict(ty, lat, n_lat, n_items, steps, counters, status, grid, barrier_extra,
                                    barrier_shift, s);
+    if (ty == 16)
+        return launch_detail::batch_launch<true, 16>(lat, n_lat, n_items, steps, counters, status, grid,
+                                                     barrier_extra, barrier_shift, s);
     if (ty == 8)
         return launch_detail::batch_launch<true, 8>(lat, n_lat, n_items, steps, counters, status, grid,
-                                                    barrier_extra, barrier_shift, s);
-    if (ty == 4)
-        return launch_detail::batch_launch<true, 4>(lat, n_lat, n_items, steps, counters, status, grid,
                                                     barrier_extra, barrier_shift, s);
     return cudaErrorInvalidValue;
 }

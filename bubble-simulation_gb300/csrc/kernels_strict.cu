@@ -46,23 +46,31 @@ namespace bubble {
 namespace launch {
 
 bool stage_shape_supported(int precision_double, int ty) {
-    return precision_double ? ty == 4 : (ty == 4 || ty == 8);
+    return precision_double ? (ty == 4 || ty == 16) : (ty == 4 || ty == 8 || ty == 16);
 }
 size_t stage_smem_bytes(int precision_double, int ty) {
-    if (precision_double) return dev::ColumnLayout<double, 4>::bytes;
+    if (precision_double) return ty == 16 ? dev::ColumnLayout<double, 16>::bytes : dev::ColumnLayout<double, 4>::bytes;
+    if (ty == 16) return dev::ColumnLayout<float, 16>::bytes;
     return ty == 4 ? dev::ColumnLayout<float, 4>::bytes : dev::ColumnLayout<float, 8>::bytes;
 }
 
-cudaError_t stage_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape,
-                                int mode, const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
+cudaError_t stage_f32_strict(const StageArgs<float> &A, const LatticeParams<float> &P, TileShape shape, int mode,
+                             const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
     using namespace launch_detail;
-    if (shape.tx != 32 || shape.ty != 8) return cudaErrorInvalidValue;
-    if (mode == dev::kThermal)
-        return stage_column<float, false, dev::kThermal, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-    if (mode == dev::kGamma) return stage_column<float, false, dev::kGamma, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-    if (mode == dev::kPert) return stage_column<float, false, dev::kPert, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-    if (mode == dev::kMixed) return stage_column<float, false, dev::kMixed, 8>(A, P, shape.lz, maps, tma_ok, status, s);
-    return stage_column<float, false, dev::kPlain, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+    if (shape.tx != tile_x_for(shape.ty)) return cudaErrorInvalidValue;
+    if (shape.ty == 16) {
+        if (mode == dev::kThermal)
+            return stage_column<float, false, dev::kThermal, 16>(A, P, shape.lz, maps, tma_ok, status, s);
+        if (mode == dev::kGamma) return stage_column<float, false, dev::kGamma, 16>(A, P, shape.lz, maps, tma_ok, status, s);
+        if (mode == dev::kPert) return stage_column<float, false, dev::kPert, 16>(A, P, shape.lz, maps, tma_ok, status, s);
+        if (mode == dev::kMixed) return stage_column<float, false, dev::kMixed, 16>(A, P, shape.lz, maps, tma_ok, status, s);
+        return stage_column<float, false, dev::kPlain, 16>(A, P, shape.lz, maps, tma_ok, status, s);
+    }
+    if (shape.ty == 8 && mode == dev::kMixed)
+        return stage_column<float, false, dev::kMixed, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+    if (shape.ty == 8 && mode == dev::kPlain)
+        return stage_column<float, false, dev::kPlain, 8>(A, P, shape.lz, maps, tma_ok, status, s);
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace launch
@@ -72,14 +80,14 @@ namespace bubble {
 namespace launch {
 
 int batch_max_grid_strict(int ty) {
-    if (ty != 8) return 0;
-    return launch_detail::batch_max_grid<false, 8>();
+    if (ty != 16) return 0;
+    return launch_detail::batch_max_grid<false, 16>();
 }
 cudaError_t batch_launch_strict(int ty, const void *lat, int n_lat, int n_items, int steps,
                                 unsigned int *counters, int *status, int grid, unsigned int barrier_extra,
                                 int barrier_shift, cudaStream_t s) {
-    if (ty != 8) return cudaErrorInvalidValue;
-    return launch_detail::batch_launch<false, 8>(lat, n_lat, n_items, steps, counters, status, grid, barrier_extra,
+    if (ty != 16) return cudaErrorInvalidValue;
+    return launch_detail::batch_launch<false, 16>(lat, n_lat, n_items, steps, counters, status, grid, barrier_extra,
                                                  barrier_shift, s);
 }
 

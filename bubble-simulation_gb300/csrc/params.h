@@ -80,4 +80,9 @@ struct TileShape {
     int32_t tx, ty, lz;  // x, y tile (cells) and z chunk (planes)
 };
 
+// The stage kernel's tiles are 16 x 16 (FP32 default: the least perimeter,
+// so the least halo work, for 256 column threads) or 32 x ty (ty = 8, 4):
+// the tile height selects the width.
+constexpr int tile_x_for(int ty) { return ty == 16 ? 16 : 32; }
+
 }  // namespace bubble

@@ -27,7 +27,7 @@ class Server {
         if (s->opt_.max_active == 0) s->opt_.max_active = 64;
         if (!(s->opt_.memory_fraction > 0.0f) || s->opt_.memory_fraction > 1.0f) s->opt_.memory_fraction = 0.85f;
         bubble_batch_options bo;
-        bo.tile_y = o.tile_y ? o.tile_y : 8;
+        bo.tile_y = o.tile_y ? o.tile_y : 16;
         bo.autotune = 0;
         bo.use_graph = o.use_graph;
         bo.max_grid = 0;
@@ -277,7 +277,7 @@ extern "C" {
 void bubble_server_options_default(bubble_server_options *out) {
     if (!out) return;
     out->math = BUBBLE_MATH_FAST;
-    out->tile_y = 8;
+    out->tile_y = 16;
     out->chunk_steps = 50;
     out->max_active = 64;
     out->memory_fraction = 0.85f;

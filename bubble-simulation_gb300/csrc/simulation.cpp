@@ -51,7 +51,8 @@ int default_chunk(const uint32_t grid[3], int ty) {
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long tiles = (long)((grid[0] + 31) / 32) * (long)((grid[1] + ty - 1) / ty);
+    const long tx = tile_x_for(ty);
+    const long tiles = (long)((grid[0] + tx - 1) / tx) * (long)((grid[1] + ty - 1) / ty);
     // Two regimes, measured (ms per step, 8 bubbles):
     //  * lattices too small to fill the GPU with 16-plane chunks are latency
     //    bound: fill one wave of two CTAs per SM with chunks of >= 8 planes
@@ -119,8 +120,8 @@ int Simulation::create(const bubble_spec &spec, std::unique_ptr<Simulation> &out
     sim->spec_ = spec;
     std::memcpy(sim->grid_, spec.grid, sizeof(sim->grid_));
     sim->n_cells_ = (uint64_t)spec.grid[0] * spec.grid[1] * spec.grid[2];
-    sim->tile_.tx = 32;
-    sim->tile_.ty = sim->is_f64() ? 4 : 8;
+    sim->tile_.ty = 16;
+    sim->tile_.tx = tile_x_for(sim->tile_.ty);
     sim->tile_.lz = default_chunk(sim->grid_, sim->tile_.ty);
     BUBBLE_CUDA(cudaStreamCreateWithFlags(&sim->stream_, cudaStreamNonBlocking), "cudaStreamCreate");
     sim->own_stream_ = true;
@@ -201,7 +202,7 @@ int Simulation::allocate(std::string &err) {
     tma_ok_ = true;
     for (int k = 0; k < 3; ++k)
         tma_ok_ = tma_ok_ && encode_stage_maps(&maps_[k], field_[k], fluid_[k], (int)grid_[0], (int)grid_[1],
-                                               (int)grid_[2], 32, tile_.ty, is_f64() ? 8 : 4);
+                                               (int)grid_[2], tile_.tx, tile_.ty, is_f64() ? 8 : 4);
     if (!h_result_) BUBBLE_CUDA(cudaMallocHost(reinterpret_cast<void **>(&h_result_), sizeof(DiagResult)), "cudaMallocHost");
     device_bytes_ = 3 * slot + scratch;
     return BUBBLE_OK;
@@ -352,11 +353,15 @@ int Simulation::resize(const uint32_t grid[3], std::string &err) {
 
 int Simulation::set_tile(TileShape t, std::string &err) {
     const bool strict = !is_f64() && spec_.math == BUBBLE_MATH_STRICT;
-    const bool pert = spec_.precision == BUBBLE_PRECISION_PERTURBATION || spec_.eos == BUBBLE_EOS_GAMMA_LAW ||
-                      spec_.eos == BUBBLE_EOS_THERMAL;
-    // the synchronous-staging and strict kernels are built for fewer shapes
-    // than the default one; their launches check the shape themselves
-    if (t.tx != 32 || !launch::stage_shape_supported(is_f64(), t.ty) || ((strict || pert) && t.ty != 8) || t.lz < 1) {
+    const bool other = spec_.precision == BUBBLE_PRECISION_PERTURBATION || spec_.eos == BUBBLE_EOS_GAMMA_LAW ||
+                       spec_.eos == BUBBLE_EOS_THERMAL;
+    // Compiled shapes: FP64 16 x 16 and 32 x 4; FP32 16 x 16 in every form and
+    // arithmetic; 32 x 8 for the plain and MIXED forms; 32 x 4 for those in
+    // the fast arithmetic.
+    bool ok = t.tx == tile_x_for(t.ty) && launch::stage_shape_supported(is_f64(), t.ty) && t.lz >= 1;
+    if (!is_f64() && other && t.ty != 16) ok = false;
+    if (strict && t.ty == 4) ok = false;
+    if (!ok) {
         err = "unsupported tile shape";
         return BUBBLE_ERR_INVALID;
     }
@@ -365,7 +370,7 @@ int Simulation::set_tile(TileShape t, std::string &err) {
         tma_ok_ = true;
         for (int k = 0; k < 3; ++k)
             tma_ok_ = tma_ok_ && encode_stage_maps(&maps_[k], field_[k], fluid_[k], (int)grid_[0], (int)grid_[1],
-                                                   (int)grid_[2], 32, t.ty, is_f64() ? 8 : 4);
+                                                   (int)grid_[2], t.tx, t.ty, is_f64() ? 8 : 4);
     }
     tile_ = t;
     return BUBBLE_OK;

@@ -2,8 +2,8 @@
 //
 // The arithmetic of the reference's primitives pass and stage pass
 // (shaders/primitives.wgsl:16-23, shaders/step.wgsl:92-174) with every face
-// flux computed once.  A CTA owns a 32 x TY column tile of the lattice and
-// marches it through a chunk of z planes:
+// flux computed once.  A CTA owns a TX x TY column tile of the lattice (16 x
+// 16, or 32 x 8 and 32 x 4) and marches it through a chunk of z planes:
 //
 //   * column threads, one per cell of the tile, keep their cell column's z
 //     direction in registers: the primitives of three planes, the upper z
@@ -43,7 +43,7 @@ namespace dev {
 
 template <typename R, int TY>
 struct ColumnLayout {
-    static constexpr int TX = 32;
+    static constexpr int TX = tile_x_for(TY);
     static constexpr int PW = TX + 4, PH = TY + 4, PC = PW * PH, NC = TX * TY;
     static constexpr int NH = 64;  // halo threads: two warps
     static constexpr int NT = NC + NH;

@@ -20,7 +20,7 @@ extern "C" {
 typedef struct bubble_batch bubble_batch;
 
 typedef struct bubble_batch_options {
-    int32_t tile_y;     /* 8 (default) or 4 (fast mode only)                  */
+    int32_t tile_y;     /* 16 (16 x 16 tiles, default) or 8 (32 x 8, fast only) */
     int32_t autotune;   /* 1: time candidate z chunks per lattice size        */
     int32_t use_graph;  /* 1: capture the launch in a CUDA graph and replay   */
     int32_t max_grid;   /* 0: every co-resident CTA; else cap on the CTAs     */

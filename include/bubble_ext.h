@@ -22,8 +22,10 @@ extern "C" {
                                    model, SINGLE and DOUBLE only)            */
 int bubble_ext_set_path(bubble_sim *sim, int32_t path);
 
-/* Tile of the fused kernel: y extent (4 or 8 for FP32, 4 for FP64; x is 32)
- * and z chunk (planes marched per CTA). */
+/* Tile of the fused kernel: y extent, which fixes the x extent (FP32: 16
+ * for 16 x 16 tiles, the default, in every form; 8 for 32 x 8 in the plain
+ * and MIXED forms; 4 for 32 x 4 in those forms with the fast arithmetic;
+ * FP64: 16 (default) or 4 for 32 x 4) and z chunk (planes marched per CTA). */
 int bubble_ext_set_tile(bubble_sim *sim, int32_t ty, int32_t lz);
 int bubble_ext_get_tile(const bubble_sim *sim, int32_t *ty, int32_t *lz);
 
@@ -47,8 +49,9 @@ void bubble_ext_inject_allocation_failure(void);
  * cycles (10..31).  Those waits expire, the CTAs set the status word and
  * return with nothing in flight, and the next bubble_synchronize or
  * bubble_diagnostics returns BUBBLE_ERR_TIMEOUT; the context stays usable.
- * Lattices whose tiles all touch the periodic boundary (x < 68 cells or
- * y < 12) have no TMA tile, and the hook then changes nothing. */
+ * Lattices whose tiles all touch the periodic boundary (with the default
+ * 16 x 16 tiles: x or y below 34 cells) have no TMA tile, and the hook then
+ * changes nothing. */
 int bubble_ext_test_expire_stage_wait(bubble_sim *sim, uint32_t extra_bytes, int32_t wait_shift);
 
 /* Raw FP64 result of the diagnostics reduction: sums over cells of the

@@ -28,7 +28,7 @@ typedef struct bubble_server bubble_server;
 
 typedef struct bubble_server_options {
     int32_t math;            /* BUBBLE_MATH_* of every request (default FAST)   */
-    int32_t tile_y;          /* 8 (default) or 4 (fast mode only)               */
+    int32_t tile_y;          /* 16 (16 x 16 tiles, default) or 8 (fast only)     */
     uint32_t chunk_steps;    /* steps per scheduling round (default 50)         */
     uint32_t max_active;     /* resident lattices at most (default 64)          */
     float memory_fraction;   /* share of free device memory a new lattice may

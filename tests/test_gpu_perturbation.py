@@ -112,7 +112,7 @@ def test_init_and_paths(bubble, gpu, tmp_path):
         f, u = s.copy_state()
         assert (u == 0).all() and (f == 0).all()
         with pytest.raises(bubble.BubbleError):
-            s.set_tile(4, 16)  # built for ty = 8 only
+            s.set_tile(4, 16)  # built for 16 x 16 tiles only
         s.set_path("reference")
         with pytest.raises(bubble.BubbleError):
             s.advance(1)  # the default kernel path only

@@ -40,8 +40,9 @@ def _spec(bubble, grid, math="strict"):
 
 def test_stage_wait_expires_and_reports_timeout(bubble, gpu, oracle_mod):
     L = bubble.load()
-    # 96 x 32 has column tiles whose halo lies inside the lattice: they stage by TMA
-    grid = (96, 32, 24)
+    # 96 x 48 has 16 x 16 column tiles whose halo lies inside the lattice:
+    # they stage by TMA
+    grid = (96, 48, 24)
     with bubble.Simulation(_spec(bubble, grid)) as sim:
         sim.advance(2)
         sim.synchronize()
