@@ -85,7 +85,7 @@ def peaks() -> tuple[float, str]:
 
 def ncu_traffic(wl: str) -> float | None:
     """DRAM bytes per cell per stage launch from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "stage_v2_traffic.txt"
+    p = ROOT / "profiles" / "stage_kernel_traffic_256cubed.txt"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -97,7 +97,7 @@ def ncu_traffic(wl: str) -> float | None:
 def ncu_flops() -> float | None:
     """FP32 operations per cell-update of the stage kernel from the committed
     ncu summary (FADD + FMUL + 2 FFMA, paired forms counted per lane), if any."""
-    p = ROOT / "profiles" / "stage_v2_flops.txt"
+    p = ROOT / "profiles" / "stage_kernel_flops_256cubed.txt"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -713,7 +713,7 @@ def main() -> int:
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic",
                 "config": {"workload": wl["name"], "grid": list(wl["grid"]), "cells": cells,
-                           "tile": [32, ty, lz], "l2": "inputs larger than L2 (no flush)",
+                           "tile": [16 if ty == 16 else 32, ty, lz], "l2": "inputs larger than L2 (no flush)",
                            "parallelism": f"replicas x{world}" if world > 1 else "single lattice"},
                 "roofline": roofline, "fp32": fp32, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": launches, "clocks": clocks.summary()}

@@ -332,13 +332,33 @@ void Batch::plan_items() {
         if (lats_[k].state && !lats_[k].solo) item_order_.push_back(k);
     std::stable_sort(item_order_.begin(), item_order_.end(),
                      [&](uint32_t a, uint32_t c) { return lats_[a].cells > lats_[c].cells; });
-    n_items_ = 0;
-    for (uint32_t k : item_order_) {
-        const Lat &L = lats_[k];
-        const int tx = tile_x_for(ty_);
-        const int tiles = (int)((L.grid[0] + tx - 1) / tx) * (int)((L.grid[1] + ty_ - 1) / ty_);
-        n_items_ += tiles * (int)((L.grid[2] + L.lz - 1) / L.lz);
+    const int tx = tile_x_for(ty_);
+    auto count_items = [&]() {
+        int n = 0;
+        for (uint32_t k : item_order_) {
+            const Lat &L = lats_[k];
+            const int tiles = (int)((L.grid[0] + tx - 1) / tx) * (int)((L.grid[1] + ty_ - 1) / ty_);
+            n += tiles * (int)((L.grid[2] + L.lz - 1) / L.lz);
+        }
+        return n;
+    };
+    if (fill_) {
+        // Equal chunks no longer than the cap; the cap halves while doubling
+        // the items still fits one wave of the persistent grid (every item
+        // then takes about half as long, and the round with it; halving
+        // past that point would add a wave).  Any chunking gives the same
+        // bits.
+        for (int cap = lz_cap_;; cap /= 2) {
+            for (uint32_t k : item_order_) {
+                Lat &L = lats_[k];
+                const int nz = (int)L.grid[2];
+                const int pieces = (nz + cap - 1) / cap;
+                L.lz = (nz + pieces - 1) / pieces;
+            }
+            if (cap / 2 < 8 || 2 * count_items() > max_grid_) break;
+        }
     }
+    n_items_ = count_items();
     grid_ = std::max(1, std::min(max_grid_, n_items_));
     dirty_ = false;
 }

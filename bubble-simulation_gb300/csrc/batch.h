@@ -94,8 +94,15 @@ class Batch {
     int check_status(std::string &err);
 
    public:
-    // z planes per work item of lattices that join later (0: 64)
-    void set_chunk_planes(int planes) { lz_cap_ = planes > 0 ? planes : 64; }
+    // z planes per work item of lattices that join later (0: 64).  A batch
+    // with a chunk cap re-chunks on every membership change: while the items
+    // of a stage would fill at most half the persistent grid, the cap halves
+    // (down to 8 planes), so a round of a few lattices still spreads over
+    // the GPU.
+    void set_chunk_planes(int planes) {
+        lz_cap_ = planes > 0 ? planes : 64;
+        fill_ = true;
+    }
     // Test hook: the next persistent launch runs its grid barrier with a
     // release count no arrival reaches and a 2^shift-cycle wait limit, so
     // every CTA's barrier wait expires and sets bit 1 of the status word.
@@ -110,6 +117,7 @@ class Batch {
     bool fast_ = true;
     int ty_ = 8;
     int lz_cap_ = 64;  // z chunk of lattices that join later
+    bool fill_ = false;  // re-chunk under lz_cap_ to fill the grid
     int grid_ = 0;
     int max_grid_ = 0;
     int n_items_ = 0;
