@@ -60,6 +60,7 @@ std::string check_spec(const bubble_spec &s, int math) {
     if (s.math != math) return "all lattices of a batch share one math mode";
     for (int a = 0; a < 3; ++a)
         if (s.grid[a] < BUBBLE_MIN_GRID || s.grid[a] > BUBBLE_MAX_GRID) return "grid axis out of 8..2048";
+    if ((uint64_t)s.grid[0] * s.grid[1] * s.grid[2] > BUBBLE_MAX_CELLS) return "lattice above 2^32 - 1 cells";
     if (s.nucleation < BUBBLE_NUCLEATION_SIMULTANEOUS || s.nucleation > BUBBLE_NUCLEATION_UNIFORM)
         return "unknown nucleation mode";
     return "";

@@ -151,6 +151,8 @@ int bubble_max_cubic_size(uint64_t max_buffer_bytes, uint64_t budget_bytes, int3
     uint32_t s = by_buffer < by_budget ? by_buffer : by_budget;
     if (s < BUBBLE_MIN_GRID) s = BUBBLE_MIN_GRID;
     if (s > BUBBLE_MAX_GRID) s = BUBBLE_MAX_GRID;
+    // and the largest cube the stage kernels' 32-bit cell index covers
+    while ((uint64_t)s * s * s > BUBBLE_MAX_CELLS) --s;
     *side = s;
     if (limited_by_memory) *limited_by_memory = by_budget < by_buffer ? 1 : 0;
     return BUBBLE_OK;

@@ -58,6 +58,10 @@ class Server {
                 err = "grid axis out of 8..2048";
                 return BUBBLE_ERR_INVALID;
             }
+        if ((uint64_t)spec.grid[0] * spec.grid[1] * spec.grid[2] > BUBBLE_MAX_CELLS) {
+            err = "lattice above 2^32 - 1 cells";
+            return BUBBLE_ERR_INVALID;
+        }
         Req r;
         r.id = next_id_++;
         r.spec = spec;

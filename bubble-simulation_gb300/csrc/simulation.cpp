@@ -40,6 +40,10 @@ std::string check_grid(const uint32_t grid[3]) {
             return "grid axis " + std::to_string(a) + " is " + std::to_string(grid[a]) +
                    "; the largest supported axis is " + std::to_string(BUBBLE_MAX_GRID);
     }
+    const uint64_t cells = (uint64_t)grid[0] * grid[1] * grid[2];
+    if (cells > BUBBLE_MAX_CELLS)
+        return "lattice of " + std::to_string(cells) + " cells; the stage kernels index at most " +
+               std::to_string(BUBBLE_MAX_CELLS) + " cells";
     return "";
 }
 

@@ -74,7 +74,7 @@ struct ColumnLayout {
 // of its six faces, its primitive q0 (sanitised), field values of its six
 // neighbours, its own U_in (pf, pu) and U^n (pfn, pun); writes U_out at g.
 template <typename R, bool FAST, int FORM>
-BUBBLE_DEV void combine_cell(const StageArgs<R> &A, const LatticeParams<R> &P, size_t g, const V4<R> &q0, R phi0,
+BUBBLE_DEV void combine_cell(const StageArgs<R> &A, const LatticeParams<R> &P, uint32_t g, const V4<R> &q0, R phi0,
                              R phxm, R phxp, R phym, R phyp, R phzm, R phzp, const V4<R> &fxm, const V4<R> &fxp,
                              const V4<R> &fym, const V4<R> &fyp, const V4<R> &fzm, const V4<R> &fzp,
                              const V2<R> &pf, const V4<R> &pu, const V2<R> &pfn, const V4<R> &pun) {
@@ -198,7 +198,8 @@ BUBBLE_DEV bool column_item(unsigned char *smem, const StageArgs<R> &A, const La
     const int xe = min(TX, P.nx - x0);
     const int ye = min(TY, P.ny - y0);
     const R zmax2 = P.z_max * P.z_max;
-    const size_t plane = (size_t)P.nx * (size_t)P.ny;
+    // cell indices fit 32 bits: the host rejects lattices of 2^32 cells or more
+    const uint32_t plane = (uint32_t)P.nx * (uint32_t)P.ny;
     const bool tma = tma_ok && x0 >= 2 && x0 + TX + 2 <= P.nx && y0 >= 2 && y0 + TY + 2 <= P.ny;
     const int zlast = z1 + 1;  // last plane whose primitives are needed
 
@@ -286,18 +287,18 @@ BUBBLE_DEV bool column_item(unsigned char *smem, const StageArgs<R> &A, const La
                 }
             }
         } else {
-            const size_t base = (size_t)gz * plane;
+            const uint32_t base = (uint32_t)gz * plane;
             if (cv) {
-                cp_async_v4(raw_u + s * PC + cc, A.fluid_in + base + c_off);
-                cp_async_v2(raw_f + s * PC + cc, A.field_in + base + c_off);
+                cp_async_v4(raw_u + s * PC + cc, A.fluid_in + (base + c_off));
+                cp_async_v2(raw_f + s * PC + cc, A.field_in + (base + c_off));
             }
             if (!col) {
                 static_for<0, L::HR>([&](auto rc) {
                     constexpr int r = decltype(rc)::value;
                     const int2 e = hr_plan[r * NH + h];
                     if (e.x >= 0) {
-                        cp_async_v4(raw_u + s * PC + e.x, A.fluid_in + base + (uint32_t)e.y);
-                        cp_async_v2(raw_f + s * PC + e.x, A.field_in + base + (uint32_t)e.y);
+                        cp_async_v4(raw_u + s * PC + e.x, A.fluid_in + (base + (uint32_t)e.y));
+                        cp_async_v2(raw_f + s * PC + e.x, A.field_in + (base + (uint32_t)e.y));
                     }
                 });
             }
@@ -331,8 +332,8 @@ BUBBLE_DEV bool column_item(unsigned char *smem, const StageArgs<R> &A, const La
     V4<R> q0{R(0), R(0), R(0), R(0)}, q1 = q0, hiz = q0, fz_m = q0;
     R ph_m = R(0), ph0 = R(0), ph1 = R(0);
     if (cv) {
-        const size_t ga = (size_t)wrap1(z0 - 2, P.nz) * plane + c_off;
-        const size_t gb = (size_t)wrap1(z0 - 1, P.nz) * plane + c_off;
+        const uint32_t ga = (uint32_t)wrap1(z0 - 2, P.nz) * plane + c_off;
+        const uint32_t gb = (uint32_t)wrap1(z0 - 1, P.nz) * plane + c_off;
         const V4<R> ua = A.fluid_in[ga], ub = A.fluid_in[gb];
         ph0 = A.field_in[ga].x;
         ph1 = A.field_in[gb].x;
@@ -414,7 +415,7 @@ BUBBLE_DEV bool column_item(unsigned char *smem, const StageArgs<R> &A, const La
         V4<R> pu{R(0), R(0), R(0), R(0)}, pun{R(0), R(0), R(0), R(0)};
         if (act) {
             if (cv) {
-                const size_t g = (size_t)z * plane + c_off;
+                const uint32_t g = (uint32_t)z * plane + c_off;
                 pf = A.field_in[g];
                 pu = A.fluid_in[g];
                 if (A.stage != 0) {
@@ -459,7 +460,7 @@ BUBBLE_DEV bool column_item(unsigned char *smem, const StageArgs<R> &A, const La
         }
         // ---- phase C: combine plane z ------------------------------------------
         if (act && cv) {
-            combine_cell<R, FAST, FORM>(A, P, (size_t)z * plane + c_off, q0, ph0, ph_z[cc - 1], ph_z[cc + 1],
+            combine_cell<R, FAST, FORM>(A, P, (uint32_t)z * plane + c_off, q0, ph0, ph_z[cc - 1], ph_z[cc + 1],
                                         ph_z[cc - PW], ph_z[cc + PW], ph_m, ph1, fxs[cj * (TX + 1) + ci],
                                         fxs[cj * (TX + 1) + ci + 1], fys[cj * TX + ci], fys[(cj + 1) * TX + ci], fz_m,
                                         fz_p, pf, pu, pfn, pun);

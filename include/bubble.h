@@ -47,6 +47,10 @@ extern "C" {
 #define BUBBLE_MIN_GRID 8u
 /* Largest axis accepted (src/gpu/sim.rs:49-51). */
 #define BUBBLE_MAX_GRID 2048u
+/* Largest lattice accepted: the stage kernels index cells in 32 bits (a
+ * lattice this large holds 309 GB of FP32 state, more than one GB300's
+ * HBM). */
+#define BUBBLE_MAX_CELLS 4294967295ull
 /* Bubbles stamped by one nucleation launch (src/gpu/sim.rs:40-41). */
 #define BUBBLE_MAX_BATCH 1024u
 
@@ -202,7 +206,9 @@ uint64_t bubble_lattice_bytes(const uint32_t grid[3]);
 uint64_t bubble_bytes_per_cell(int32_t precision);
 /* Simulation::max_cubic_size (src/gpu/sim.rs:717-733): the largest cubic
  * side allowed by a per-buffer limit (bytes of one 16 B/cell fluid slot) and
- * an optional memory budget (bubble_lattice_bytes per cell). */
+ * an optional memory budget (bubble_lattice_bytes per cell), clamped to
+ * [BUBBLE_MIN_GRID, BUBBLE_MAX_GRID] as there and, beyond the reference, to
+ * 1625, the largest cube within BUBBLE_MAX_CELLS. */
 int bubble_max_cubic_size(uint64_t max_buffer_bytes, uint64_t budget_bytes,
                           int32_t has_budget, uint32_t *side,
                           int32_t *limited_by_memory);

@@ -146,6 +146,8 @@ def test_max_cubic_size(bubble):
     assert bubble.lattice_bytes((tight,) * 3) <= 1_000_000_000
     assert bubble.max_cubic_size(2_147_483_648, None)[0] == side
     assert bubble.max_cubic_size(1024, 1024)[0] == 8
+    # beyond the reference's 2048-cell axis cap: the 32-bit cell index
+    assert bubble.max_cubic_size(1 << 62, None)[0] == 1625
 
 
 # src/gpu/vram.rs:162-207
@@ -181,6 +183,16 @@ def test_no_device_means_loud_failure(bubble):
     with pytest.raises(bubble.BubbleError) as e:
         bubble.Simulation(bubble.SimulationSpec(grid=(16, 16, 16)))
     assert e.value.code == bubble._lib.ERR_CUDA
+
+
+def test_lattice_above_32_bit_cell_index_is_rejected(bubble):
+    """The stage kernels index cells in 32 bits: a lattice of 2^32 cells or
+    more is refused before any device work (2048 x 2048 x 1024 is exactly
+    2^32), while the axis limit alone would accept it."""
+    with pytest.raises(bubble.BubbleError) as e:
+        bubble.Simulation(bubble.SimulationSpec(grid=(2048, 2048, 1024)))
+    assert e.value.code == bubble._lib.ERR_INVALID
+    assert "4294967296 cells" in str(e.value)
 
 
 # ---- CLI (src/config.rs:209-242, src/main.rs) -------------------------------
