@@ -64,6 +64,10 @@ __global__ void __launch_bounds__(ColumnLayout<float, TY>::NT, ColumnLayout<floa
                     unsigned int *counters, int *status, unsigned int barrier_extra, int barrier_shift) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int item_s;
+    // the current item's stage arguments and lattice constants, read from
+    // shared memory by the item body instead of held in registers
+    __shared__ StageArgs<float> A_s;
+    __shared__ LatticeParams<float> P_s;
     unsigned int round = 0;
     // Every CTA ends a round with one grab past the last item, so a round
     // consumes exactly n_items + gridDim.x grabs of the counter.
@@ -90,20 +94,26 @@ __global__ void __launch_bounds__(ColumnLayout<float, TY>::NT, ColumnLayout<floa
                 const int a = cur, b = (cur + 1) % 3, c = (cur + 2) % 3;
                 const int in_slot = stage == 0 ? a : (stage == 1 ? b : c);
                 const int out_slot = stage == 1 ? c : b;
-                StageArgs<float> A;
-                A.field_n = B.field[a];
-                A.fluid_n = B.fluid[a];
-                A.field_in = B.field[in_slot];
-                A.fluid_in = B.fluid[in_slot];
-                A.field_out = B.field[out_slot];
-                A.fluid_out = B.fluid[out_slot];
-                // the RK3 table (src/gpu/sim.rs:133-135) as selects, not an indexed array
-                A.a0 = stage == 0 ? 0.0f : (stage == 1 ? 0.75f : 1.0f / 3.0f);
-                A.a1 = stage == 0 ? 1.0f : (stage == 1 ? 0.25f : 2.0f / 3.0f);
-                A.dt = B.dt;
-                A.stage = stage;
-                const LatticeParams<float> P = B.P;
-                if (!column_item<float, FAST, kPlain, TY>(smem, A, P, B.lz, &B.maps[in_slot], B.tma_ok, status,
+                // Thread 0 publishes the item's arguments: every thread has
+                // left the previous item (the barriers above), and
+                // column_item's opening barrier makes them visible.
+                if (threadIdx.x == 0) {
+                    StageArgs<float> A;
+                    A.field_n = B.field[a];
+                    A.fluid_n = B.fluid[a];
+                    A.field_in = B.field[in_slot];
+                    A.fluid_in = B.fluid[in_slot];
+                    A.field_out = B.field[out_slot];
+                    A.fluid_out = B.fluid[out_slot];
+                    // the RK3 table (src/gpu/sim.rs:133-135) as selects, not an indexed array
+                    A.a0 = stage == 0 ? 0.0f : (stage == 1 ? 0.75f : 1.0f / 3.0f);
+                    A.a1 = stage == 0 ? 1.0f : (stage == 1 ? 0.25f : 2.0f / 3.0f);
+                    A.dt = B.dt;
+                    A.stage = stage;
+                    A_s = A;
+                    P_s = B.P;
+                }
+                if (!column_item<float, FAST, kPlain, TY>(smem, A_s, P_s, B.lz, &B.maps[in_slot], B.tma_ok, status,
                                                       local % B.tiles_xy, local / B.tiles_xy)) {
                     // record where the stage's bounded wait gave up (status[8..12])
                     if (threadIdx.x == 0 && atomicCAS(&status[8], 0, 1) == 0) {
