@@ -216,6 +216,11 @@ class Simulation:
     def set_tile(self, ty: int, lz: int):
         check(self._L.bubble_ext_set_tile(self._h, ty, lz))
 
+    def set_stage_form(self, form: str):
+        """Form of the fused kernel for FP32 16 x 16 tiles: "auto" (default),
+        "registers" or "shared" (identical bits; include/bubble_ext.h)."""
+        check(self._L.bubble_ext_set_stage_form(self._h, _lib.STAGE_FORMS[form]))
+
     def tile(self) -> tuple[int, int]:
         ty, lz = ctypes.c_int32(), ctypes.c_int32()
         check(self._L.bubble_ext_get_tile(self._h, ctypes.byref(ty), ctypes.byref(lz)))

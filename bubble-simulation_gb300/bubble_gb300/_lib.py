@@ -31,6 +31,7 @@ EOS = {"bag": 0, "bag_dof": 1, "gamma_law": 2, "thermal": 3}
 PATH_FUSED = 0
 PATH_REFERENCE = 1
 PATHS = {"fused": PATH_FUSED, "reference": PATH_REFERENCE}
+STAGE_FORMS = {"auto": 0, "registers": 1, "shared": 2}
 MIN_GRID = 8
 MAX_GRID = 2048
 MAX_BATCH = 1024
@@ -184,6 +185,7 @@ SIGNATURES = [
     ("bubble_ext_set_path", ctypes.c_int, [_P, ctypes.c_int32]),
     ("bubble_ext_set_tile", ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
     ("bubble_ext_get_tile", ctypes.c_int, [_P, _I32P, _I32P]),
+    ("bubble_ext_set_stage_form", ctypes.c_int, [_P, ctypes.c_int32]),
     ("bubble_ext_device_state", ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P)]),
     ("bubble_ext_stream", _P, [_P]),
     ("bubble_ext_launches", ctypes.c_uint64, [_P]),

@@ -56,10 +56,17 @@ BUBBLE_DEV bool grid_barrier(unsigned int *count, unsigned int *gen, int *status
     return ok_s != 0;
 }
 
+// The batch's items run the shared form of the column kernel with 16 x 16
+// tiles (three CTAs per SM: 43.6 against 42.1 solves/s on the 64-lattice
+// mixed-size batch), the register form with 32 x 8 tiles.
+template <int TY>
+constexpr bool kBatchShared = TY == 16;
+
 // sync: counters[0] = barrier count, counters[1] = barrier generation,
 //       counters[2] = work counter (zeroed before the launch).
 template <bool FAST, int TY>
-__global__ void __launch_bounds__(ColumnLayout<float, TY>::NT, ColumnLayout<float, TY>::MIN_BLOCKS)
+__global__ void __launch_bounds__(ColumnLayout<float, TY, kBatchShared<TY>>::NT,
+                                  ColumnLayout<float, TY, kBatchShared<TY>>::MIN_BLOCKS)
     batch_kernel(const BatchLattice *__restrict__ lat, int n_lat, int n_items, int steps,
                     unsigned int *counters, int *status, unsigned int barrier_extra, int barrier_shift) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -113,7 +120,7 @@ __global__ void __launch_bounds__(ColumnLayout<float, TY>::NT, ColumnLayout<floa
                     A_s = A;
                     P_s = B.P;
                 }
-                if (!column_item<float, FAST, kPlain, TY>(smem, A_s, P_s, B.lz, &B.maps[in_slot], B.tma_ok, status,
+                if (!column_item<float, FAST, kPlain, TY, kBatchShared<TY>>(smem, A_s, P_s, B.lz, &B.maps[in_slot], B.tma_ok, status,
                                                       local % B.tiles_xy, local / B.tiles_xy)) {
                     // record where the stage's bounded wait gave up (status[8..12])
                     if (threadIdx.x == 0 && atomicCAS(&status[8], 0, 1) == 0) {

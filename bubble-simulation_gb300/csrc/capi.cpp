@@ -304,6 +304,9 @@ int bubble_ext_test_expire_stage_wait(bubble_sim *sim, uint32_t extra_bytes, int
 int bubble_ext_set_tile(bubble_sim *sim, int32_t ty, int32_t lz) {
     SIM_CALL(sim->impl->set_tile(bubble::TileShape{bubble::tile_x_for(ty), ty, lz}, err));
 }
+int bubble_ext_set_stage_form(bubble_sim *sim, int32_t form) {
+    SIM_CALL(sim->impl->set_stage_form(form, err));
+}
 int bubble_ext_get_tile(const bubble_sim *sim, int32_t *ty, int32_t *lz) {
     if (!sim || !sim->impl) return fail(BUBBLE_ERR_INVALID, "sim is NULL");
     const bubble::TileShape t = sim->impl->tile();

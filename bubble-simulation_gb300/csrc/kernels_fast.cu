@@ -11,11 +11,11 @@ cudaError_t stage_f32_fast(const StageArgs<float> &A, const LatticeParams<float>
     using namespace launch_detail;
     if (shape.tx != tile_x_for(shape.ty)) return cudaErrorInvalidValue;
     if (shape.ty == 16) {
-        if (mode == dev::kThermal) return stage_column<float, true, dev::kThermal, 16>(A, P, shape.lz, maps, tma_ok, status, s);
-        if (mode == dev::kGamma) return stage_column<float, true, dev::kGamma, 16>(A, P, shape.lz, maps, tma_ok, status, s);
-        if (mode == dev::kPert) return stage_column<float, true, dev::kPert, 16>(A, P, shape.lz, maps, tma_ok, status, s);
-        if (mode == dev::kMixed) return stage_column<float, true, dev::kMixed, 16>(A, P, shape.lz, maps, tma_ok, status, s);
-        return stage_column<float, true, dev::kPlain, 16>(A, P, shape.lz, maps, tma_ok, status, s);
+        if (mode == dev::kThermal) return stage_column16<true, dev::kThermal>(A, P, shape, maps, tma_ok, status, s);
+        if (mode == dev::kGamma) return stage_column16<true, dev::kGamma>(A, P, shape, maps, tma_ok, status, s);
+        if (mode == dev::kPert) return stage_column16<true, dev::kPert>(A, P, shape, maps, tma_ok, status, s);
+        if (mode == dev::kMixed) return stage_column16<true, dev::kMixed>(A, P, shape, maps, tma_ok, status, s);
+        return stage_column16<true, dev::kPlain>(A, P, shape, maps, tma_ok, status, s);
     }
     if (mode != dev::kPlain && mode != dev::kMixed) return cudaErrorInvalidValue;
     if (shape.ty == 8) {
@@ -42,7 +42,8 @@ int batch_max_grid(bool fast, int ty) {
     return 0;
 }
 size_t batch_smem_bytes(int ty) {
-    return ty == 16 ? dev::ColumnLayout<float, 16>::bytes : dev::ColumnLayout<float, 8>::bytes;
+    return ty == 16 ? dev::ColumnLayout<float, 16, dev::kBatchShared<16>>::bytes
+                    : dev::ColumnLayout<float, 8, dev::kBatchShared<8>>::bytes;
 }
 cudaError_t batch_launch(bool fast, int ty, const void *lat, int n_lat, int n_items, int steps,
                          unsigned int *counters, int *status, int grid, unsigned int barrier_extra,

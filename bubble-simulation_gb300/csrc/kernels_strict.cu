@@ -60,11 +60,11 @@ cudaError_t stage_f32_strict(const StageArgs<float> &A, const LatticeParams<floa
     if (shape.tx != tile_x_for(shape.ty)) return cudaErrorInvalidValue;
     if (shape.ty == 16) {
         if (mode == dev::kThermal)
-            return stage_column<float, false, dev::kThermal, 16>(A, P, shape.lz, maps, tma_ok, status, s);
-        if (mode == dev::kGamma) return stage_column<float, false, dev::kGamma, 16>(A, P, shape.lz, maps, tma_ok, status, s);
-        if (mode == dev::kPert) return stage_column<float, false, dev::kPert, 16>(A, P, shape.lz, maps, tma_ok, status, s);
-        if (mode == dev::kMixed) return stage_column<float, false, dev::kMixed, 16>(A, P, shape.lz, maps, tma_ok, status, s);
-        return stage_column<float, false, dev::kPlain, 16>(A, P, shape.lz, maps, tma_ok, status, s);
+            return stage_column16<false, dev::kThermal>(A, P, shape, maps, tma_ok, status, s);
+        if (mode == dev::kGamma) return stage_column16<false, dev::kGamma>(A, P, shape, maps, tma_ok, status, s);
+        if (mode == dev::kPert) return stage_column16<false, dev::kPert>(A, P, shape, maps, tma_ok, status, s);
+        if (mode == dev::kMixed) return stage_column16<false, dev::kMixed>(A, P, shape, maps, tma_ok, status, s);
+        return stage_column16<false, dev::kPlain>(A, P, shape, maps, tma_ok, status, s);
     }
     if (shape.ty == 8 && mode == dev::kMixed)
         return stage_column<float, false, dev::kMixed, 8>(A, P, shape.lz, maps, tma_ok, status, s);

@@ -7,6 +7,7 @@
 #include <utility>
 #include <vector>
 
+#include "bubble_ext.h"
 #include "kernels.cuh"
 #include "launch.h"
 #include "stage_column.cuh"
@@ -84,11 +85,11 @@ cudaError_t stage_ref(const StageArgs<R> &A, const V4<R> *prim, const LatticePar
     return cudaGetLastError();
 }
 
-template <typename R, bool FAST, int FORM, int TY>
+template <typename R, bool FAST, int FORM, int TY, bool LEAN = false>
 cudaError_t stage_column(const StageArgs<R> &A, const LatticeParams<R> &P, int lz, const StageMaps &maps, int tma_ok,
                      int *status, cudaStream_t s) {
-    using L = dev::ColumnLayout<R, TY>;
-    auto k = dev::stage_kernel<R, FAST, FORM, TY>;
+    using L = dev::ColumnLayout<R, TY, LEAN>;
+    auto k = dev::stage_kernel<R, FAST, FORM, TY, LEAN>;
     cudaError_t e = ensure_smem(k, L::bytes);
     if (e != cudaSuccess) return e;
     if (lz < 1) lz = 1;
@@ -97,6 +98,34 @@ cudaError_t stage_column(const StageArgs<R> &A, const LatticeParams<R> &P, int l
     dim3 grid(ntx * nty, nzc);
     k<<<grid, L::NT, L::bytes, s>>>(A, P, lz, maps, tma_ok, status);
     return cudaGetLastError();
+}
+
+// Whether a 16 x 16 FP32 stage launch takes the shared form: on request, or
+// (BUBBLE_STAGE_FORM_AUTO) when the launch has at least two waves of three
+// CTAs per SM.  Measured per step, register vs shared form: 128^3 (256 CTAs)
+// 0.239 vs 0.261 ms, 256^3 (2048 CTAs) 1.549 vs 1.508 ms, 512^3 (4096 CTAs)
+// 11.38 vs 11.03 ms.
+inline bool shared_form(const LatticeParams<float> &P, const TileShape &shape) {
+    if (shape.form == BUBBLE_STAGE_FORM_SHARED) return true;
+    if (shape.form == BUBBLE_STAGE_FORM_REGISTERS) return false;
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0, n = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        sms = n > 0 ? n : 1;
+    }
+    const int lz = shape.lz < 1 ? 1 : shape.lz;
+    const long ctas = (long)((P.nx + 15) / 16) * (long)((P.ny + 15) / 16) * (long)((P.nz + lz - 1) / lz);
+    return ctas >= 6L * sms;
+}
+
+// A 16 x 16 FP32 stage launch in the form shared_form() picks.
+template <bool FAST, int FORM>
+cudaError_t stage_column16(const StageArgs<float> &A, const LatticeParams<float> &P, const TileShape &shape,
+                           const StageMaps &maps, int tma_ok, int *status, cudaStream_t s) {
+    if (shared_form(P, shape)) return stage_column<float, FAST, FORM, 16, true>(A, P, shape.lz, maps, tma_ok, status, s);
+    return stage_column<float, FAST, FORM, 16, false>(A, P, shape.lz, maps, tma_ok, status, s);
 }
 
 template <typename R, int MIXED>
@@ -119,7 +148,7 @@ namespace launch_detail {
 
 template <bool FAST, int TY>
 int batch_max_grid() {
-    using L = dev::ColumnLayout<float, TY>;
+    using L = dev::ColumnLayout<float, TY, dev::kBatchShared<TY>>;
     auto k = dev::batch_kernel<FAST, TY>;
     if (ensure_smem(k, L::bytes) != cudaSuccess) return 0;
     int dev = 0, sms = 0, per_sm = 0;
@@ -132,7 +161,7 @@ int batch_max_grid() {
 template <bool FAST, int TY>
 cudaError_t batch_launch(const void *lat, int n_lat, int n_items, int steps, unsigned int *counters,
                          int *status, int grid, unsigned int barrier_extra, int barrier_shift, cudaStream_t s) {
-    using L = dev::ColumnLayout<float, TY>;
+    using L = dev::ColumnLayout<float, TY, dev::kBatchShared<TY>>;
     auto k = dev::batch_kernel<FAST, TY>;
     cudaError_t e = ensure_smem(k, L::bytes);
     if (e != cudaSuccess) return e;

@@ -78,6 +78,7 @@ struct DiagResult {
 // Tile shape of the fused stage kernel.
 struct TileShape {
     int32_t tx, ty, lz;  // x, y tile (cells) and z chunk (planes)
+    int32_t form = 0;    // BUBBLE_STAGE_FORM_* of 16 x 16 FP32 launches
 };
 
 // The stage kernel's tiles are 16 x 16 (FP32 default: the least perimeter,

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "../../include/bubble_ext.h"
 #include "launch.h"
 
 namespace bubble {
@@ -376,7 +377,17 @@ int Simulation::set_tile(TileShape t, std::string &err) {
             tma_ok_ = tma_ok_ && encode_stage_maps(&maps_[k], field_[k], fluid_[k], (int)grid_[0], (int)grid_[1],
                                                    (int)grid_[2], t.tx, t.ty, is_f64() ? 8 : 4);
     }
+    t.form = tile_.form;
     tile_ = t;
+    return BUBBLE_OK;
+}
+
+int Simulation::set_stage_form(int form, std::string &err) {
+    if (form != BUBBLE_STAGE_FORM_AUTO && form != BUBBLE_STAGE_FORM_REGISTERS && form != BUBBLE_STAGE_FORM_SHARED) {
+        err = "unknown stage form";
+        return BUBBLE_ERR_INVALID;
+    }
+    tile_.form = form;
     return BUBBLE_OK;
 }
 

@@ -61,7 +61,9 @@ class Simulation {
         test_shift_ = shift;
     }
     KernelPath path() const { return path_; }
-    int set_tile(TileShape t, std::string &err);
+    int set_tile(TileShape t, std::string &err);  // keeps the stage form
+    // BUBBLE_STAGE_FORM_* of FP32 16 x 16 launches
+    int set_stage_form(int form, std::string &err);
     TileShape tile() const { return tile_; }
 
     float time() const { return time_; }

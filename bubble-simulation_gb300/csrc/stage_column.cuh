@@ -15,6 +15,19 @@
 //   * two halo warps recover the cross-shaped halo ring of each plane and
 //     compute the face states and fluxes on the tile's far edges.
 //
+// Two forms of the same arithmetic (template flag LEAN):
+//   * register form: the column's z pipeline (the primitives and phi of the
+//     planes around z, the carried upper z face state and the lower z flux)
+//     stays in registers: 83 registers, two CTAs per SM;
+//   * shared form: the column thread reads its own primitives and phi back
+//     from the staged rings (where they are stored anyway) and keeps the
+//     carried z state and the lower z flux in per-thread shared slots: 64
+//     registers, three CTAs per SM.  Each of those accesses is by the owning
+//     thread, so no barrier is added.  Faster where the launch fills several
+//     waves (3.1 % at 512^3), slower on small lattices that cannot fill the
+//     third CTA slot.
+// Both forms evaluate every value by the same operations: identical bits.
+//
 // Per plane z, three phases and two barriers:
 //   A  recover plane z+2 (column cells into registers and shared memory,
 //      halo ring into shared memory); z face states of plane z+1 and the z
@@ -41,13 +54,13 @@
 namespace bubble {
 namespace dev {
 
-template <typename R, int TY>
+template <typename R, int TY, bool LEAN = false>
 struct ColumnLayout {
     static constexpr int TX = tile_x_for(TY);
     static constexpr int PW = TX + 4, PH = TY + 4, PC = PW * PH, NC = TX * TY;
     static constexpr int NH = 64;  // halo threads: two warps
     static constexpr int NT = NC + NH;
-    static constexpr int MIN_BLOCKS = sizeof(R) == 4 ? 2 : 1;
+    static constexpr int MIN_BLOCKS = sizeof(R) == 4 ? (LEAN ? 3 : 2) : 1;
     static constexpr int HR = (4 * (TX + TY) + NH - 1) / NH;  // halo cells recovered per halo thread
     static constexpr int HS = (2 * (TX + TY) + NH - 1) / NH;  // halo face states per halo thread
     static_assert(TX + TY <= NH && TY <= 32, "one halo flux per halo thread, x faces on the second warp");
@@ -65,7 +78,11 @@ struct ColumnLayout {
     // per halo thread: HR (cell, in-plane offset) pairs, HS (cell, stride,
     // destination, upper) quadruples, written once per item
     static constexpr size_t o_plan = align128(o_fy + (TY + 1) * TX * sizeof(V4<R>));
-    static constexpr size_t o_bar = o_plan + NH * (HR * 2 + HS * 4) * sizeof(int);
+    // shared form: per column thread, the upper z face state it carries and
+    // the flux of its lower z face
+    static constexpr size_t o_hz = align128(o_plan + NH * (HR * 2 + HS * 4) * sizeof(int));
+    static constexpr size_t o_fz = o_hz + (LEAN ? NC * sizeof(V4<R>) : 0);
+    static constexpr size_t o_bar = o_fz + (LEAN ? NC * sizeof(V4<R>) : 0);
     static constexpr size_t bytes = o_bar + 2 * sizeof(uint64_t);
     static constexpr uint32_t plane_tx_bytes = PC * (sizeof(V4<R>) + sizeof(V2<R>));
 };
@@ -171,10 +188,10 @@ BUBBLE_DEV void combine_cell(const StageArgs<R> &A, const LatticeParams<R> &P, u
 // when a bounded wait expired (bit 0 of *status is set); the CTA must then
 // stop.  Usable repeatedly by one CTA: it starts with a barrier and leaves
 // no copy in flight.
-template <typename R, bool FAST, int FORM, int TY>
+template <typename R, bool FAST, int FORM, int TY, bool LEAN = false>
 BUBBLE_DEV bool column_item(unsigned char *smem, const StageArgs<R> &A, const LatticeParams<R> &P, int lz,
                         const StageMaps *maps, int tma_ok, int *status, int tile_xy, int chunk) {
-    using L = ColumnLayout<R, TY>;
+    using L = ColumnLayout<R, TY, LEAN>;
     constexpr int TX = L::TX, NC = L::NC, NH = L::NH, PW = L::PW, PC = L::PC;
     __syncthreads();  // a previous item on this CTA is done with shared memory
     V4<R> *raw_u = reinterpret_cast<V4<R> *>(smem + L::o_rawu);
@@ -188,6 +205,8 @@ BUBBLE_DEV bool column_item(unsigned char *smem, const StageArgs<R> &A, const La
     V4<R> *fxs = reinterpret_cast<V4<R> *>(smem + L::o_fx);   // [j][i]: flux of face i-1/2
     V4<R> *fys = reinterpret_cast<V4<R> *>(smem + L::o_fy);   // [j][i]: flux of face j-1/2
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::o_bar);
+    V4<R> *hz_s = reinterpret_cast<V4<R> *>(smem + L::o_hz);  // shared form: [t] carried upper z state
+    V4<R> *fz_s = reinterpret_cast<V4<R> *>(smem + L::o_fz);  // shared form: [t] flux of face z-1/2
 
     const int t = threadIdx.x;
     const int ntx = (P.nx + TX - 1) / TX;
@@ -325,20 +344,32 @@ BUBBLE_DEV bool column_item(unsigned char *smem, const StageArgs<R> &A, const La
     issue(z0);
     issue(z0 + 1);  // zlast >= z0 + 2
 
-    // The z pipeline of a column: q0, q1 = primitives of planes z, z+1;
-    // ph_m .. ph1 = phi of planes z-1 .. z+1; hiz = upper z state of cell z;
-    // fz_m = flux of face z-1/2.  The warm-up planes z0-2, z0-1 come
-    // straight from global memory.
+    // The z pipeline of a column (register form): q0, q1 = primitives of
+    // planes z, z+1; ph_m .. ph1 = phi of planes z-1 .. z+1; hiz = upper z
+    // state of cell z; fz_m = flux of face z-1/2.  The shared form reads the
+    // same values from the rings and from hz_s / fz_s.  The warm-up planes
+    // z0-2, z0-1 come straight from global memory.
     V4<R> q0{R(0), R(0), R(0), R(0)}, q1 = q0, hiz = q0, fz_m = q0;
     R ph_m = R(0), ph0 = R(0), ph1 = R(0);
     if (cv) {
         const uint32_t ga = (uint32_t)wrap1(z0 - 2, P.nz) * plane + c_off;
         const uint32_t gb = (uint32_t)wrap1(z0 - 1, P.nz) * plane + c_off;
         const V4<R> ua = A.fluid_in[ga], ub = A.fluid_in[gb];
-        ph0 = A.field_in[ga].x;
-        ph1 = A.field_in[gb].x;
-        q0 = recover_sanitised<R, FAST, FORM>(ua, P, ph0, zmax2);
-        q1 = recover_sanitised<R, FAST, FORM>(ub, P, ph1, zmax2);
+        const R pa = A.field_in[ga].x, pb = A.field_in[gb].x;
+        const V4<R> qa = recover_sanitised<R, FAST, FORM>(ua, P, pa, zmax2);
+        const V4<R> qb = recover_sanitised<R, FAST, FORM>(ub, P, pb, zmax2);
+        if constexpr (LEAN) {
+            prim_slot(z0 - 2)[cc] = qa;
+            prim_slot(z0 - 1)[cc] = qb;
+            phi_slot(z0 - 2)[cc] = pa;
+            phi_slot(z0 - 1)[cc] = pb;
+            hz_s[t] = V4<R>{R(0), R(0), R(0), R(0)};
+        } else {
+            q0 = qa;
+            q1 = qb;
+            ph0 = pa;
+            ph1 = pb;
+        }
     }
     {
         const bool to = !wait_raw(z0, true);
@@ -384,15 +415,26 @@ BUBBLE_DEV bool column_item(unsigned char *smem, const StageArgs<R> &A, const La
         V4<R> fz_p{R(0), R(0), R(0), R(0)}, lox, loy;
         if (cv) {
             // z face states of cell z+1 and the flux of face z+1/2
+            V4<R> c0 = q0, c1 = q1;
+            if constexpr (LEAN) {
+                c0 = pr_z[cc];
+                c1 = prim_slot(z + 1)[cc];
+            }
             V4<R> lo1, hi1;
-            face_states<R, FAST>(q0, q1, q2, P.p_floor, zmax2, lo1, hi1);
-            if (z >= z0 - 1) fz_p = hll_flux<2, R, FAST, FORM>(hiz, lo1, zmax2, P, ph0, ph1);
-            hiz = hi1;
+            face_states<R, FAST>(c0, c1, q2, P.p_floor, zmax2, lo1, hi1);
+            if constexpr (LEAN) {
+                if (z >= z0 - 1)
+                    fz_p = hll_flux<2, R, FAST, FORM>(hz_s[t], lo1, zmax2, P, ph_z[cc], phi_slot(z + 1)[cc]);
+                hz_s[t] = hi1;
+            } else {
+                if (z >= z0 - 1) fz_p = hll_flux<2, R, FAST, FORM>(hiz, lo1, zmax2, P, ph0, ph1);
+                hiz = hi1;
+            }
             if (act) {
                 V4<R> hix, hiy;
-                face_states<R, FAST>(pr_z[cc - 1], q0, pr_z[cc + 1], P.p_floor, zmax2, lox, hix);
+                face_states<R, FAST>(pr_z[cc - 1], c0, pr_z[cc + 1], P.p_floor, zmax2, lox, hix);
                 hxs[cj * (TX + 1) + ci + 1] = hix;
-                face_states<R, FAST>(pr_z[cc - PW], q0, pr_z[cc + PW], P.p_floor, zmax2, loy, hiy);
+                face_states<R, FAST>(pr_z[cc - PW], c0, pr_z[cc + PW], P.p_floor, zmax2, loy, hiy);
                 hys[(cj + 1) * TX + ci] = hiy;
             }
         }
@@ -427,8 +469,10 @@ BUBBLE_DEV bool column_item(unsigned char *smem, const StageArgs<R> &A, const La
                     phl_x = ph_z[cc - 1];
                     phl_y = ph_z[cc - PW];
                 }
-                fxs[cj * (TX + 1) + ci] = hll_flux<0, R, FAST, FORM>(hxs[cj * (TX + 1) + ci], lox, zmax2, P, phl_x, ph0);
-                fys[cj * TX + ci] = hll_flux<1, R, FAST, FORM>(hys[cj * TX + ci], loy, zmax2, P, phl_y, ph0);
+                R phc = ph0;
+                if constexpr (LEAN) phc = ph_z[cc];
+                fxs[cj * (TX + 1) + ci] = hll_flux<0, R, FAST, FORM>(hxs[cj * (TX + 1) + ci], lox, zmax2, P, phl_x, phc);
+                fys[cj * TX + ci] = hll_flux<1, R, FAST, FORM>(hys[cj * TX + ci], loy, zmax2, P, phl_y, phc);
             } else if (!col) {
                 if (h < 32) {
                     // y face above row ye-1, column h
@@ -459,28 +503,39 @@ BUBBLE_DEV bool column_item(unsigned char *smem, const StageArgs<R> &A, const La
             return false;
         }
         // ---- phase C: combine plane z ------------------------------------------
-        if (act && cv) {
-            combine_cell<R, FAST, FORM>(A, P, (uint32_t)z * plane + c_off, q0, ph0, ph_z[cc - 1], ph_z[cc + 1],
-                                        ph_z[cc - PW], ph_z[cc + PW], ph_m, ph1, fxs[cj * (TX + 1) + ci],
-                                        fxs[cj * (TX + 1) + ci + 1], fys[cj * TX + ci], fys[(cj + 1) * TX + ci], fz_m,
-                                        fz_p, pf, pu, pfn, pun);
+        if constexpr (LEAN) {
+            if (act && cv) {
+                combine_cell<R, FAST, FORM>(A, P, (uint32_t)z * plane + c_off, pr_z[cc], ph_z[cc], ph_z[cc - 1],
+                                            ph_z[cc + 1], ph_z[cc - PW], ph_z[cc + PW], phi_slot(z - 1)[cc],
+                                            phi_slot(z + 1)[cc], fxs[cj * (TX + 1) + ci],
+                                            fxs[cj * (TX + 1) + ci + 1], fys[cj * TX + ci], fys[(cj + 1) * TX + ci],
+                                            fz_s[t], fz_p, pf, pu, pfn, pun);
+            }
+            if (cv) fz_s[t] = fz_p;
+        } else {
+            if (act && cv) {
+                combine_cell<R, FAST, FORM>(A, P, (uint32_t)z * plane + c_off, q0, ph0, ph_z[cc - 1], ph_z[cc + 1],
+                                            ph_z[cc - PW], ph_z[cc + PW], ph_m, ph1, fxs[cj * (TX + 1) + ci],
+                                            fxs[cj * (TX + 1) + ci + 1], fys[cj * TX + ci], fys[(cj + 1) * TX + ci],
+                                            fz_m, fz_p, pf, pu, pfn, pun);
+            }
+            q0 = q1;
+            q1 = q2;
+            ph_m = ph0;
+            ph0 = ph1;
+            ph1 = ph2;
+            fz_m = fz_p;
         }
-        q0 = q1;
-        q1 = q2;
-        ph_m = ph0;
-        ph0 = ph1;
-        ph1 = ph2;
-        fz_m = fz_p;
     }
     return true;
 }
 
-template <typename R, bool FAST, int FORM, int TY>
-__global__ void __launch_bounds__(ColumnLayout<R, TY>::NT, ColumnLayout<R, TY>::MIN_BLOCKS)
+template <typename R, bool FAST, int FORM, int TY, bool LEAN>
+__global__ void __launch_bounds__(ColumnLayout<R, TY, LEAN>::NT, ColumnLayout<R, TY, LEAN>::MIN_BLOCKS)
     stage_kernel(StageArgs<R> A, LatticeParams<R> P, int lz, const __grid_constant__ StageMaps maps,
                     int tma_ok, int *status) {
     extern __shared__ __align__(128) unsigned char smem[];
-    column_item<R, FAST, FORM, TY>(smem, A, P, lz, &maps, tma_ok, status, blockIdx.x, blockIdx.y);
+    column_item<R, FAST, FORM, TY, LEAN>(smem, A, P, lz, &maps, tma_ok, status, blockIdx.x, blockIdx.y);
 }
 
 }  // namespace dev

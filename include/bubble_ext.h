@@ -29,6 +29,17 @@ int bubble_ext_set_path(bubble_sim *sim, int32_t path);
 int bubble_ext_set_tile(bubble_sim *sim, int32_t ty, int32_t lz);
 int bubble_ext_get_tile(const bubble_sim *sim, int32_t *ty, int32_t *lz);
 
+/* Form of the fused kernel for FP32 16 x 16 tiles; both forms give
+ * identical bits.  REGISTERS keeps each column's z pipeline in registers
+ * (two CTAs per SM); SHARED reads it back from shared memory (three CTAs
+ * per SM, faster once a launch fills several waves); AUTO (default) takes
+ * SHARED for launches of at least six CTAs per SM.  Other tiles and FP64
+ * always use REGISTERS. */
+#define BUBBLE_STAGE_FORM_AUTO 0
+#define BUBBLE_STAGE_FORM_REGISTERS 1
+#define BUBBLE_STAGE_FORM_SHARED 2
+int bubble_ext_set_stage_form(bubble_sim *sim, int32_t form);
+
 /* Device pointers of the current slot U^n (valid until the next step). */
 int bubble_ext_device_state(bubble_sim *sim, void **field, void **fluid);
 /* The cudaStream_t the simulation launches on. */

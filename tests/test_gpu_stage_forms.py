@@ -1,0 +1,118 @@
+"""The two forms of the fused stage kernel give identical bits.
+
+For 16 x 16 FP32 tiles the stage kernel comes in two forms of the same
+arithmetic (include/bubble_ext.h BUBBLE_STAGE_FORM_*):
+- The register form keeps a column's z pipeline in registers, two CTAs per
+  SM.
+- The shared form reads the pipeline back from shared memory, three CTAs
+  per SM.
+
+AUTO picks by launch size; these tests force each form.
+
+Checked here:
+- Every FP32 form (plain, MIXED, perturbation, gamma-law and thermal
+  equations of state) in both arithmetic modes, on shocked states and, for
+  MIXED, on a state above gamma = 3, gives bit-identical results in both
+  forms.
+- The lattices have TMA-staged interior tiles and boundary tiles.
+- The shared form gives the same bits under several z chunkings.
+- The strict shared form matches the oracle directly.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import make_golden
+
+pytestmark = pytest.mark.gpu
+
+GRIDS = [(48, 40, 36), (33, 17, 20)]
+E_REF = 0.125  # e_ref of the default model
+
+
+def _state(oracle_mod, grid, seed, kind, eos=None):
+    sched = oracle_mod.make_schedule("centre", 1, 5.0, grid, 10.0, 1)
+    kw = {"eos": eos} if eos else {}
+    o = oracle_mod.OracleSim(grid, schedule=sched, precision="mixed" if kind == "mixed" else "f32", **kw)
+    o.advance(4)
+    if kind == "mixed":
+        make_golden.relativistic_state(o, seed, 0.995)
+    else:
+        make_golden.perturbed_state(o, seed, 0.3)
+    f, u = o.state()
+    if kind == "perturbation":
+        u = u.copy()
+        u[:, 0] = (u[:, 0] - np.float32(o.d["e_ref"])).astype(np.float32)  # stored form: E - e_ref
+    return f, u
+
+
+def _run(bubble, grid, f0, u0, steps, form, math, precision="single", eos="bag", eos_param=(1.0, 0.0), lz=None):
+    spec = bubble.SimulationSpec(grid=grid, bubbles=0, nucleation="centre", precision=precision, math=math,
+                                 eos=eos, eos_param=eos_param)
+    with bubble.Simulation(spec) as sim:
+        sim.set_stage_form(form)
+        if lz is not None:
+            sim.set_tile(16, lz)
+        sim.load_state(f0, u0)
+        sim.advance(steps)
+        return sim.copy_state()
+
+
+def _same(a, b, what):
+    bad = np.argwhere(np.asarray(a) != np.asarray(b))
+    assert bad.size == 0, f"{what}: {len(bad)} differing values, first {bad[:3].tolist()}"
+
+
+CASES = [
+    # (state kind, precision, eos, eos_param, oracle eos)
+    ("plain", "single", "bag", (1.0, 0.0), None),
+    ("mixed", "mixed", "bag", (1.0, 0.0), None),
+    ("perturbation", "perturbation", "bag", (1.0, 0.0), None),
+    ("plain", "single", "gamma_law", (1.2, 0.05), ("gamma_law", 1.2, 0.05)),
+    ("plain", "single", "thermal", (E_REF / 6.0, E_REF / np.sqrt(2.0)), ("thermal", E_REF / 6.0, E_REF / np.sqrt(2.0))),
+]
+
+
+@pytest.mark.parametrize("math", ["strict", "fast"])
+@pytest.mark.parametrize("case", CASES, ids=[f"{c[1]}-{c[2]}" for c in CASES])
+@pytest.mark.parametrize("grid", GRIDS)
+def test_forms_bit_identical(bubble, oracle_mod, gpu, grid, case, math):
+    kind, precision, eos, param, oeos = case
+    f0, u0 = _state(oracle_mod, grid, 7, kind, oeos)
+    kw = dict(precision=precision, eos=eos, eos_param=param)
+    fr, ur = _run(bubble, grid, f0, u0, 6, "registers", math, **kw)
+    fs, us = _run(bubble, grid, f0, u0, 6, "shared", math, **kw)
+    assert np.isfinite(fr).all() and np.isfinite(ur).all()
+    _same(fs, fr, "field")
+    _same(us, ur, "fluid")
+
+
+@pytest.mark.parametrize("math", ["strict", "fast"])
+def test_shared_form_chunkings(bubble, oracle_mod, gpu, math):
+    grid = (48, 40, 36)
+    f0, u0 = _state(oracle_mod, grid, 8, "mixed")
+    ref = _run(bubble, grid, f0, u0, 5, "shared", math, precision="mixed", lz=grid[2])
+    for lz in (1, 5, 12):
+        f, u = _run(bubble, grid, f0, u0, 5, "shared", math, precision="mixed", lz=lz)
+        _same(f, ref[0], f"field lz {lz}")
+        _same(u, ref[1], f"fluid lz {lz}")
+
+
+def test_shared_form_strict_matches_oracle(bubble, oracle_mod, gpu):
+    grid = (48, 40, 36)
+    f0, u0 = _state(oracle_mod, grid, 9, "plain")
+    o = oracle_mod.OracleSim(grid, precision="f32")
+    o.set_state(f0, u0)
+    o.advance(6)
+    fo, uo = o.state()
+    f, u = _run(bubble, grid, f0, u0, 6, "shared", "strict")
+    _same(f, fo, "field")
+    _same(u, uo, "fluid")
+
+
+def test_unknown_form_is_rejected(bubble, gpu):
+    with bubble.Simulation(bubble.SimulationSpec(grid=(16, 16, 16))) as sim:
+        with pytest.raises(bubble.BubbleError) as e:
+            bubble._lib.check(sim._L.bubble_ext_set_stage_form(sim._h, 3))
+        assert e.value.code == bubble._lib.ERR_INVALID
