@@ -159,18 +159,21 @@ BUBBLE_DEV V4<R> prim_from_cons(const V4<R> &u, const LatticeParams<R> &P) {
 
 // FP64 recovery of one FP32 cell, used where the Lorentz factor exceeds 3
 // (v^2 > 8/9), the regime where E^2 - Z^2 cancels.  Rarely taken and long
-// (FP64 division and square root are multi-instruction sequences), so each
-// kernel holds one out-of-line copy instead of one per recovery site (measured
-// at 512^3: 1.6 % faster, fewer instruction-fetch stalls); it takes the FP32
-// state and constants by value.
+// (FP64 division and square root are multi-instruction sequences).  It takes
+// the FP32 state and constants by value, so it can also be compiled out of
+// line (BUBBLE_F64_RECOVERY_LINKAGE): one copy per kernel was 1.6 % faster
+// for the register-form stage kernel at 512^3 (fewer instruction-fetch
+// stalls), inlined is 0.6 % faster for the shared form, which now runs every
+// large lattice.
+#define BUBBLE_F64_RECOVERY_LINKAGE __device__ __forceinline__
 template <bool FAST = false>
-__device__ __noinline__ V4<float> prim_from_cons_f64_x(V4<float> u, float e_floor, float z_max, float p_floor);
+BUBBLE_F64_RECOVERY_LINKAGE V4<float> prim_from_cons_f64_x(V4<float> u, float e_floor, float z_max, float p_floor);
 template <bool FAST = false>
 BUBBLE_DEV V4<float> prim_from_cons_f64(const V4<float> &u, const LatticeParams<float> &P) {
     return prim_from_cons_f64_x<FAST>(u, P.e_floor, P.z_max, P.p_floor);
 }
 template <bool FAST>
-__device__ __noinline__ V4<float> prim_from_cons_f64_x(V4<float> u, float e_floor_f, float z_max_f, float p_floor_f) {
+BUBBLE_F64_RECOVERY_LINKAGE V4<float> prim_from_cons_f64_x(V4<float> u, float e_floor_f, float z_max_f, float p_floor_f) {
     struct {
         float e_floor, z_max, p_floor;
     } P{e_floor_f, z_max_f, p_floor_f};
@@ -259,17 +262,17 @@ BUBBLE_DEV V4<R> prim_from_cons_pert(const V4<R> &u, const LatticeParams<R> &P) 
     }
 }
 
-// FP64 recovery of one FP32 cell in the perturbation form (gamma > 3), out
-// of line like prim_from_cons_f64.
+// FP64 recovery of one FP32 cell in the perturbation form (gamma > 3),
+// compiled like prim_from_cons_f64.
 template <bool FAST = false>
-__device__ __noinline__ V4<float> prim_from_cons_pert_f64_x(V4<float> u, float e_floor, float z_max, float p_floor,
+BUBBLE_F64_RECOVERY_LINKAGE V4<float> prim_from_cons_pert_f64_x(V4<float> u, float e_floor, float z_max, float p_floor,
                                                             float e_bg, float p_bg);
 template <bool FAST = false>
 BUBBLE_DEV V4<float> prim_from_cons_pert_f64(const V4<float> &u, const LatticeParams<float> &P) {
     return prim_from_cons_pert_f64_x<FAST>(u, P.e_floor, P.z_max, P.p_floor, P.e_bg, P.p_bg);
 }
 template <bool FAST>
-__device__ __noinline__ V4<float> prim_from_cons_pert_f64_x(V4<float> u, float e_floor_f, float z_max_f,
+BUBBLE_F64_RECOVERY_LINKAGE V4<float> prim_from_cons_pert_f64_x(V4<float> u, float e_floor_f, float z_max_f,
                                                             float p_floor_f, float e_bg_f, float p_bg_f) {
     struct {
         float e_floor, z_max, p_floor, e_bg, p_bg;
