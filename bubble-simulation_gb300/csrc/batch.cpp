@@ -293,7 +293,7 @@ int Batch::add(const bubble_spec &spec, uint32_t *index, std::string &err) {
         const long tiles = (long)((L.grid[0] + tx - 1) / tx) * (long)((L.grid[1] + ty_ - 1) / ty_);
         L.solo = tiles * (((long)L.grid[2] + 31) / 32) >= 2L * std::max(sms, 1);
         if (L.solo) {
-            L.lz = default_chunk(L.grid, ty_);
+            L.lz = default_chunk(L.grid, ty_, true);
         } else {
             // equal chunks no longer than the cap
             const int nz = (int)L.grid[2];

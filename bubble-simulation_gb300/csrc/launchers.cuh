@@ -101,10 +101,10 @@ cudaError_t stage_column(const StageArgs<R> &A, const LatticeParams<R> &P, int l
 }
 
 // Whether a 16 x 16 FP32 stage launch takes the shared form: on request, or
-// (BUBBLE_STAGE_FORM_AUTO) when the launch has at least two waves of three
-// CTAs per SM.  Measured per step, register vs shared form: 128^3 (256 CTAs)
-// 0.239 vs 0.261 ms, 256^3 (2048 CTAs) 1.549 vs 1.508 ms, 512^3 (4096 CTAs)
-// 11.38 vs 11.03 ms.
+// (BUBBLE_STAGE_FORM_AUTO) when column_stage_cost (params.h) rates it cheaper
+// at this chunk.  Measured per step, register vs shared form: 128^3 (256
+// CTAs) 0.239 vs 0.261 ms, 256^3 (2048 CTAs) 1.549 vs 1.508 ms, 512^3 (4096
+// CTAs) 11.38 vs 11.03 ms.
 inline bool shared_form(const LatticeParams<float> &P, const TileShape &shape) {
     if (shape.form == BUBBLE_STAGE_FORM_SHARED) return true;
     if (shape.form == BUBBLE_STAGE_FORM_REGISTERS) return false;
@@ -115,9 +115,8 @@ inline bool shared_form(const LatticeParams<float> &P, const TileShape &shape) {
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
         sms = n > 0 ? n : 1;
     }
-    const int lz = shape.lz < 1 ? 1 : shape.lz;
-    const long ctas = (long)((P.nx + 15) / 16) * (long)((P.ny + 15) / 16) * (long)((P.nz + lz - 1) / lz);
-    return ctas >= 6L * sms;
+    const uint32_t nx = (uint32_t)P.nx, ny = (uint32_t)P.ny, nz = (uint32_t)P.nz;
+    return column_stage_cost(nx, ny, nz, shape.lz, true, sms) < column_stage_cost(nx, ny, nz, shape.lz, false, sms);
 }
 
 // A 16 x 16 FP32 stage launch in the form shared_form() picks.

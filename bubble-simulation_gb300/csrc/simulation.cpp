@@ -52,15 +52,33 @@ std::string check_grid(const uint32_t grid[3]) {
 
 void inject_allocation_failure() { g_fail_next_alloc.store(1); }
 
-int default_chunk(const uint32_t grid[3], int ty) {
+int default_chunk(const uint32_t grid[3], int ty, bool fp32) {
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (fp32 && ty == 16) {
+        // the cheapest (chunk, form) of the cost model; ties go to longer
+        // chunks (fewer warm-up planes)
+        double best = 1e300;
+        int best_lz = (int)grid[2];
+        const int max_chunks = ((int)grid[2] + 7) / 8;
+        for (int chunks = 1; chunks <= max_chunks; ++chunks) {
+            const int lz = ((int)grid[2] + chunks - 1) / chunks;
+            const double c = std::min(column_stage_cost(grid[0], grid[1], grid[2], lz, false, sms),
+                                      column_stage_cost(grid[0], grid[1], grid[2], lz, true, sms));
+            if (c < best * (1.0 - 1e-9)) {
+                best = c;
+                best_lz = lz;
+            }
+        }
+        return best_lz;
+    }
     const long tx = tile_x_for(ty);
     const long tiles = (long)((grid[0] + tx - 1) / tx) * (long)((grid[1] + ty - 1) / ty);
-    // Two regimes, measured (ms per step, 8 bubbles):
+    // Other tiles and FP64, two regimes (measured with 32 x 8 tiles, ms per
+    // step, 8 bubbles):
     //  * lattices too small to fill the GPU with 16-plane chunks are latency
-    //    bound: fill one wave of two CTAs per SM with chunks of >= 8 planes
+    //    bound: one wave of two CTAs per SM with chunks of >= 8 planes
     //    (48^3: lz 8 0.062, 16 0.105, 48 0.277; 64^3: 8 0.062, 16 0.105,
     //    32 0.194; 96^3: 12 0.116, 16 0.146, 32 0.197);
     //  * larger lattices: aim at >= 24 CTAs per SM over the launch (about a
@@ -71,7 +89,9 @@ int default_chunk(const uint32_t grid[3], int ty) {
     const long resident = 2L * sms;
     long lz;
     if (tiles * (((long)grid[2] + 15) / 16) < resident) {
-        const long chunks = (resident + tiles - 1) / tiles;
+        // as many chunks as fit in one wave (rounding up would spill a few
+        // CTAs into a second one)
+        const long chunks = std::max(1L, resident / tiles);
         lz = ((long)grid[2] + chunks - 1) / chunks;
         if (lz < 8) lz = 8;
     } else {
@@ -127,7 +147,7 @@ int Simulation::create(const bubble_spec &spec, std::unique_ptr<Simulation> &out
     sim->n_cells_ = (uint64_t)spec.grid[0] * spec.grid[1] * spec.grid[2];
     sim->tile_.ty = 16;
     sim->tile_.tx = tile_x_for(sim->tile_.ty);
-    sim->tile_.lz = default_chunk(sim->grid_, sim->tile_.ty);
+    sim->tile_.lz = default_chunk(sim->grid_, sim->tile_.ty, !sim->is_f64());
     BUBBLE_CUDA(cudaStreamCreateWithFlags(&sim->stream_, cudaStreamNonBlocking), "cudaStreamCreate");
     sim->own_stream_ = true;
     int rc = sim->allocate(err);
@@ -347,7 +367,7 @@ int Simulation::resize(const uint32_t grid[3], std::string &err) {
     spec_.grid[1] = grid[1];
     spec_.grid[2] = grid[2];
     n_cells_ = (uint64_t)grid[0] * grid[1] * grid[2];
-    tile_.lz = default_chunk(grid_, tile_.ty);
+    tile_.lz = default_chunk(grid_, tile_.ty, !is_f64());
     int rc = allocate(err);
     if (rc != BUBBLE_OK) return rc;
     const Derived d = derive(spec_.model);

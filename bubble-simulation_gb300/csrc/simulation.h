@@ -166,10 +166,11 @@ LatticeParams<float> lattice_params_f32(const bubble_spec &spec);
 LatticeParams<double> lattice_params_f64(const bubble_spec &spec);
 int arith_mode(const bubble_spec &spec);
 
-// Default z chunk of the fused kernel for a lattice: enough CTAs to fill the
-// GPU several times over while keeping the 4-plane warm-up of each chunk a
+// Default z chunk of the fused kernel for a lattice.  FP32 16 x 16 tiles:
+// the chunk whose cheaper form is cheapest under column_stage_cost (params.h);
+// otherwise enough CTAs to fill the GPU while keeping each chunk's warm-up a
 // small fraction of its work.
-int default_chunk(const uint32_t grid[3], int ty);
+int default_chunk(const uint32_t grid[3], int ty, bool fp32);
 
 // Test hook: make the next device allocation of this process fail.
 void inject_allocation_failure();

@@ -32,8 +32,9 @@ int bubble_ext_get_tile(const bubble_sim *sim, int32_t *ty, int32_t *lz);
 /* Form of the fused kernel for FP32 16 x 16 tiles; both forms give
  * identical bits.  REGISTERS keeps each column's z pipeline in registers
  * (two CTAs per SM); SHARED reads it back from shared memory (three CTAs
- * per SM, faster once a launch fills several waves); AUTO (default) takes
- * SHARED for launches of at least six CTAs per SM.  Other tiles and FP64
+ * per SM, faster once a launch fills more than one wave); AUTO (default)
+ * takes the form a cost model of the launch rates cheaper for the lattice
+ * and chunk (the model also picks the default chunk).  Other tiles and FP64
  * always use REGISTERS. */
 #define BUBBLE_STAGE_FORM_AUTO 0
 #define BUBBLE_STAGE_FORM_REGISTERS 1

@@ -116,3 +116,33 @@ def test_unknown_form_is_rejected(bubble, gpu):
         with pytest.raises(bubble.BubbleError) as e:
             bubble._lib.check(sim._L.bubble_ext_set_stage_form(sim._h, 3))
         assert e.value.code == bubble._lib.ERR_INVALID
+
+
+def _stage_cost(n, lz, shared, sms):
+    # the cost model of csrc/params.h column_stage_cost, restated for a cube
+    tiles = ((n + 15) // 16) ** 2
+    chunks = (n + lz - 1) // lz
+    lz_eff = (n + chunks - 1) // chunks
+    k, p = (3, 1.45) if shared else (2, 1.0)
+    m = (tiles * chunks + sms - 1) // sms
+    rounds = (m + k - 1) // k
+    last = m - (rounds - 1) * k
+    p_last = p if last == k else (0.6 * p if last == 1 else 0.8 * p)
+    return ((rounds - 1) * p + p_last) * (lz_eff + 2)
+
+
+@pytest.mark.parametrize("n", [32, 64, 96, 128, 160, 192, 256])
+def test_default_chunk_follows_cost_model(bubble, gpu, n):
+    """The default chunk of an FP32 lattice is the cheapest under the stage
+    cost model (ties to the longer chunk) for this device's SM count."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    best, best_lz = None, n
+    for chunks in range(1, (n + 7) // 8 + 1):
+        lz = (n + chunks - 1) // chunks
+        c = min(_stage_cost(n, lz, False, sms), _stage_cost(n, lz, True, sms))
+        if best is None or c < best * (1 - 1e-9):
+            best, best_lz = c, lz
+    with bubble.Simulation(bubble.SimulationSpec(grid=(n, n, n), bubbles=1, nucleation="centre")) as sim:
+        assert sim.tile() == (16, best_lz)
