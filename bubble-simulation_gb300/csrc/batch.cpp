@@ -344,20 +344,40 @@ void Batch::plan_items() {
         return n;
     };
     if (fill_) {
-        // Equal chunks no longer than the cap; the cap halves while doubling
-        // the items still fits one wave of the persistent grid (every item
-        // then takes about half as long, and the round with it; halving
-        // past that point would add a wave).  Any chunking gives the same
-        // bits.
-        for (int cap = lz_cap_;; cap /= 2) {
+        // Equal chunks no longer than the cap, the cap chosen among the
+        // configured one and shorter ones by a cost per stage round: the
+        // item-planes (each chunk's planes plus 2 warm-up planes) spread
+        // over the persistent grid, plus the longest item (the round's
+        // tail).  Any chunking gives the same bits.
+        auto apply = [&](int cap) {
             for (uint32_t k : item_order_) {
                 Lat &L = lats_[k];
                 const int nz = (int)L.grid[2];
                 const int pieces = (nz + cap - 1) / cap;
                 L.lz = (nz + pieces - 1) / pieces;
             }
-            if (cap / 2 < 8 || 2 * count_items() > max_grid_) break;
+        };
+        double best = 1e300;
+        int best_cap = lz_cap_;
+        for (int cap : {lz_cap_, 48, 32, 24, 16, 12, 8}) {
+            if (cap > lz_cap_) continue;
+            apply(cap);
+            double planes = 0.0;
+            int longest = 0;
+            for (uint32_t k : item_order_) {
+                const Lat &L = lats_[k];
+                const long tiles = (long)((L.grid[0] + tx - 1) / tx) * (long)((L.grid[1] + ty_ - 1) / ty_);
+                const long chunks = ((long)L.grid[2] + L.lz - 1) / L.lz;
+                planes += (double)tiles * (double)(L.grid[2] + 2 * chunks);
+                longest = std::max(longest, L.lz + 2);
+            }
+            const double cost = planes / (double)std::max(1, max_grid_) + (double)longest;
+            if (cost < best * (1.0 - 1e-9)) {
+                best = cost;
+                best_cap = cap;
+            }
         }
+        apply(best_cap);
     }
     n_items_ = count_items();
     grid_ = std::max(1, std::min(max_grid_, n_items_));

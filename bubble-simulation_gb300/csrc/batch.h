@@ -95,10 +95,11 @@ class Batch {
 
    public:
     // z planes per work item of lattices that join later (0: 64).  A batch
-    // with a chunk cap re-chunks on every membership change: while the items
-    // of a stage would fill at most half the persistent grid, the cap halves
-    // (down to 8 planes), so a round of a few lattices still spreads over
-    // the GPU.
+    // with a chunk cap re-chunks on every membership change: among the cap
+    // and shorter caps (48 .. 8 planes) it takes the one with the least cost
+    // per round (the item-planes spread over the persistent grid plus the
+    // longest item), so a round of a few lattices still spreads over the
+    // GPU and a full one is not cut finer than it pays.
     void set_chunk_planes(int planes) {
         lz_cap_ = planes > 0 ? planes : 64;
         fill_ = true;

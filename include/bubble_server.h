@@ -44,9 +44,9 @@ typedef struct bubble_server_options {
                                 (cells x steps) first                            */
     uint32_t chunk_planes;   /* z planes per work item of a lattice (0: 64);
                                 columns are cut into equal chunks no longer
-                                than this; while the active lattices' items
-                                would fill at most half the persistent grid
-                                the cap halves (down to 8 planes)               */
+                                than this or a shorter cap (48 .. 8 planes)
+                                that a cost model of the round rates cheaper
+                                for the active lattices                          */
 } bubble_server_options;
 
 #define BUBBLE_SERVE_FIFO 0
