@@ -99,7 +99,7 @@ int autotune_chunk(const uint32_t grid[3], int ty, bool fast, std::string &err) 
     }
     const int nz = (int)grid[2];
     std::vector<int> cand;
-    for (int lz : {8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256})
+    for (int lz : {4, 6, 8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256})
         if (lz < nz) cand.push_back(lz);
     cand.push_back(nz);
     int best = cand.front();
@@ -359,7 +359,7 @@ void Batch::plan_items() {
         };
         double best = 1e300;
         int best_cap = lz_cap_;
-        for (int cap : {lz_cap_, 48, 32, 24, 16, 12, 8}) {
+        for (int cap : {lz_cap_, 48, 32, 24, 16, 12, 8, 6, 4}) {
             if (cap > lz_cap_) continue;
             apply(cap);
             double planes = 0.0;

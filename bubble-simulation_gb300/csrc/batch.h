@@ -96,7 +96,7 @@ class Batch {
    public:
     // z planes per work item of lattices that join later (0: 64).  A batch
     // with a chunk cap re-chunks on every membership change: among the cap
-    // and shorter caps (48 .. 8 planes) it takes the one with the least cost
+    // and shorter caps (48 .. 4 planes) it takes the one with the least cost
     // per round (the item-planes spread over the persistent grid plus the
     // longest item), so a round of a few lattices still spreads over the
     // GPU and a full one is not cut finer than it pays.

@@ -88,12 +88,13 @@ constexpr int tile_x_for(int ty) { return ty == 16 ? 16 : 32; }
 
 // Cost model of one stage launch of the 16 x 16 FP32 column kernel, in plane
 // times of a CTA that shares its SM with one other.  The register form holds
-// two CTAs per SM, the shared form three, each then 1.45x slower per plane;
+// two CTAs per SM, the shared form three, each then 1.4x slower per plane;
 // the busiest SM (ceil(CTAs / SMs) CTAs) runs them in rounds, a last round
-// of one CTA at 0.6x and of two (shared form) at 0.8x of the full round's
-// plane time; a chunk costs its planes plus 2 for its warm-up.  Fitted to 60
-// measured (form, chunk) pairs at 96^3 .. 256^3, where the cheapest pick is
-// within 1 % of the fastest measured at every size.
+// of one CTA at 0.65x and of two (shared form) at 0.8x of the full round's
+// plane time; a chunk costs its planes plus 2 for its warm-up.  Fitted to
+// about 150 measured (form, chunk) pairs from 32^3 to 512^3: the cheapest
+// pick (chunks of 4 planes or more) is the fastest measured or within 0.6 %
+// of it at every size.
 inline double column_stage_cost(uint32_t nx, uint32_t ny, uint32_t nz, int lz, bool shared, int sms) {
     if (lz < 1) lz = 1;
     if (sms < 1) sms = 1;
@@ -101,11 +102,11 @@ inline double column_stage_cost(uint32_t nx, uint32_t ny, uint32_t nz, int lz, b
     const long chunks = ((long)nz + lz - 1) / lz;
     const long lz_eff = ((long)nz + chunks - 1) / chunks;
     const long k = shared ? 3 : 2;
-    const double p = shared ? 1.45 : 1.0;
+    const double p = shared ? 1.4 : 1.0;
     const long m = (tiles * chunks + sms - 1) / sms;
     const long rounds = (m + k - 1) / k;
     const long last = m - (rounds - 1) * k;
-    const double p_last = last == k ? p : (last == 1 ? 0.6 * p : 0.8 * p);
+    const double p_last = last == k ? p : (last == 1 ? 0.65 * p : 0.8 * p);
     return ((double)(rounds - 1) * p + p_last) * (double)(lz_eff + 2);
 }
 

@@ -61,7 +61,7 @@ int default_chunk(const uint32_t grid[3], int ty, bool fp32) {
         // chunks (fewer warm-up planes)
         double best = 1e300;
         int best_lz = (int)grid[2];
-        const int max_chunks = ((int)grid[2] + 7) / 8;
+        const int max_chunks = ((int)grid[2] + 3) / 4;  // chunks of >= 4 planes
         for (int chunks = 1; chunks <= max_chunks; ++chunks) {
             const int lz = ((int)grid[2] + chunks - 1) / chunks;
             const double c = std::min(column_stage_cost(grid[0], grid[1], grid[2], lz, false, sms),

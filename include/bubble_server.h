@@ -44,7 +44,7 @@ typedef struct bubble_server_options {
                                 (cells x steps) first                            */
     uint32_t chunk_planes;   /* z planes per work item of a lattice (0: 64);
                                 columns are cut into equal chunks no longer
-                                than this or a shorter cap (48 .. 8 planes)
+                                than this or a shorter cap (48 .. 4 planes)
                                 that a cost model of the round rates cheaper
                                 for the active lattices                          */
 } bubble_server_options;

@@ -123,11 +123,11 @@ def _stage_cost(n, lz, shared, sms):
     tiles = ((n + 15) // 16) ** 2
     chunks = (n + lz - 1) // lz
     lz_eff = (n + chunks - 1) // chunks
-    k, p = (3, 1.45) if shared else (2, 1.0)
+    k, p = (3, 1.4) if shared else (2, 1.0)
     m = (tiles * chunks + sms - 1) // sms
     rounds = (m + k - 1) // k
     last = m - (rounds - 1) * k
-    p_last = p if last == k else (0.6 * p if last == 1 else 0.8 * p)
+    p_last = p if last == k else (0.65 * p if last == 1 else 0.8 * p)
     return ((rounds - 1) * p + p_last) * (lz_eff + 2)
 
 
@@ -139,7 +139,7 @@ def test_default_chunk_follows_cost_model(bubble, gpu, n):
 
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     best, best_lz = None, n
-    for chunks in range(1, (n + 7) // 8 + 1):
+    for chunks in range(1, (n + 3) // 4 + 1):
         lz = (n + chunks - 1) // chunks
         c = min(_stage_cost(n, lz, False, sms), _stage_cost(n, lz, True, sms))
         if best is None or c < best * (1 - 1e-9):
