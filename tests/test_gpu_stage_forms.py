@@ -131,10 +131,9 @@ def _stage_cost(n, lz, shared, sms):
     return ((rounds - 1) * p + p_last) * (lz_eff + 2)
 
 
-@pytest.mark.parametrize("n", [32, 64, 96, 128, 160, 192, 256])
-def test_default_chunk_follows_cost_model(bubble, gpu, n):
-    """The default chunk of an FP32 lattice is the cheapest under the stage
-    cost model (ties to the longer chunk) for this device's SM count."""
+def _model_chunk(n):
+    """The cheapest chunk of an n^3 lattice under the stage cost model (ties
+    to the longer chunk) for this device's SM count."""
     import torch
 
     sms = torch.cuda.get_device_properties(0).multi_processor_count
@@ -144,5 +143,36 @@ def test_default_chunk_follows_cost_model(bubble, gpu, n):
         c = min(_stage_cost(n, lz, False, sms), _stage_cost(n, lz, True, sms))
         if best is None or c < best * (1 - 1e-9):
             best, best_lz = c, lz
+    return best_lz
+
+
+@pytest.mark.parametrize("n", [32, 64, 96, 128, 160, 192, 256])
+def test_default_chunk_follows_cost_model(bubble, gpu, n):
+    """The default chunk of an FP32 lattice is the model's cheapest."""
     with bubble.Simulation(bubble.SimulationSpec(grid=(n, n, n), bubbles=1, nucleation="centre")) as sim:
-        assert sim.tile() == (16, best_lz)
+        assert sim.tile() == (16, _model_chunk(n))
+
+
+def test_auto_configuration_at_128_cubed(bubble, oracle_mod, gpu):
+    """At 128^3 on 152 SMs the AUTO rule runs the shared form with 19-plane
+    chunks (448 CTAs, TMA-staged interior tiles, uneven chunk ends). Strict MIXED there
+    must match the oracle bit for bit, and fast MIXED must equal the register
+    form with 32-plane chunks."""
+    grid = (128, 128, 128)
+    f0, u0 = _state(oracle_mod, grid, 10, "mixed")
+    o = oracle_mod.OracleSim(grid, precision="mixed")
+    o.set_state(f0, u0)
+    o.advance(3)
+    fo, uo = o.state()
+    spec = bubble.SimulationSpec(grid=grid, bubbles=0, nucleation="centre", precision="mixed", math="strict")
+    with bubble.Simulation(spec) as sim:
+        assert sim.tile() == (16, _model_chunk(128))
+        sim.load_state(f0, u0)
+        sim.advance(3)
+        f, u = sim.copy_state()
+    _same(f, fo, "strict field")
+    _same(u, uo, "strict fluid")
+    auto = _run(bubble, grid, f0, u0, 3, "auto", "fast", precision="mixed")
+    regs = _run(bubble, grid, f0, u0, 3, "registers", "fast", precision="mixed", lz=32)
+    _same(auto[0], regs[0], "fast field")
+    _same(auto[1], regs[1], "fast fluid")
