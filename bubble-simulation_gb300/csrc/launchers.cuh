@@ -108,13 +108,10 @@ cudaError_t stage_column(const StageArgs<R> &A, const LatticeParams<R> &P, int l
 inline bool shared_form(const LatticeParams<float> &P, const TileShape &shape) {
     if (shape.form == BUBBLE_STAGE_FORM_SHARED) return true;
     if (shape.form == BUBBLE_STAGE_FORM_REGISTERS) return false;
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0, n = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        sms = n > 0 ? n : 1;
-    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);  // the current device's
+    if (sms < 1) sms = 1;
     const uint32_t nx = (uint32_t)P.nx, ny = (uint32_t)P.ny, nz = (uint32_t)P.nz;
     return column_stage_cost(nx, ny, nz, shape.lz, true, sms) < column_stage_cost(nx, ny, nz, shape.lz, false, sms);
 }
