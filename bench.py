@@ -1,7 +1,7 @@
 """Benchmark of the GB300 lattice time step.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload precision512|default128|plain64|profile256|batch64|serve|serve_light|precision_study]
+                    [--workload precision512|default128|plain64|profile256|batch64|profile_batch64|serve|serve_light|precision_study]
 
 Metric: cell-updates/s (one cell-update = one full SSP-RK3 step of one
 cell), on the 512^3 precision-study workload by default: periodic 512^3
@@ -354,6 +354,32 @@ def batch_specs(bubble, n: int, seed: int = 20251203):
     return specs
 
 
+def run_batch_profile(args) -> int:
+    """Small case of the batched ensemble for a profiler: the batch64 lattices,
+    direct launches (no CUDA graph), no autotuning, a few steps per launch."""
+    import torch
+    import bubble_gb300 as bubble
+
+    bubble.load()
+    specs = batch_specs(bubble, args.lattices)
+    cells = sum(s.grid[0] ** 3 for s in specs)
+    b = bubble.Batch(specs, autotune=False, use_graph=False)
+    b.advance(2)  # nucleation and a first launch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        b.advance(5)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    info = b.info()
+    b.close()
+    print(json.dumps({"metric": "cell-updates/s", "value": cells * 15 / dt, "unit": "cell-updates/s",
+                      "impl": "gb300-batch-profile", "config": {"workload": f"{args.lattices} lattices of the "
+                      "batch64 workload, direct launches, no autotuning, 3 launches of 5 steps", "cells": cells},
+                      "batch_info": info}), flush=True)
+    return 0
+
+
 def run_batch(args) -> int:
     """Batched ensemble (solves/s): one persistent graph-captured launch per
     chunk of steps for all lattices, against the same plain kernels run one
@@ -600,6 +626,8 @@ def main() -> int:
     ap.add_argument("--study-steps", type=int, default=3000, help="precision_study workload: steps")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.workload == "profile_batch64":
+        return run_batch_profile(args)
     if args.workload == "batch64":
         return run_batch(args)
     if args.workload in SERVE_EDGES:
